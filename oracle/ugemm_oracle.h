@@ -1,0 +1,36 @@
+/*
+ * ugemm_oracle.h -- CPU oracle for the ugemm SGEMM path (test infrastructure
+ * only: used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg; never linked into the product library).
+ */
+#ifndef UGEMM_ORACLE_H
+#define UGEMM_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int oracle_sgemm_cpu(char major, char ta, char tb, int M, int N, int K, float alpha,
+                     const float *A, int lda, const float *B, int ldb, float beta,
+                     float *C, int ldc);
+int oracle_dgemm_cpu(char major, char ta, char tb, int M, int N, int K, double alpha,
+                     const double *A, int lda, const double *B, int ldb, double beta,
+                     double *C, int ldc);
+int oracle_sgemm_c(char major, char ta, char tb, int M, int N, int K, float alpha,
+                   const float *A, int lda, const float *B, int ldb, float beta,
+                   float *C, int ldc);
+int oracle_dgemm_c(char major, char ta, char tb, int M, int N, int K, double alpha,
+                   const double *A, int lda, const double *B, int ldb, double beta,
+                   double *C, int ldc);
+void oracle_sgemm_avx256(int M, int N, int K, float alpha, const float *A, int lda,
+                         const float *B, int ldb, float beta, float *C, int ldc);
+int oracle_sgemm_avx256_mt(int nthreads, char ta, char tb, int M, int N, int K, float alpha,
+                           const float *A, int lda, const float *B, int ldb, float beta,
+                           float *C, int ldc);
+int oracle_cmp_results(int M, int N, const float *ref, const float *res, int ld, double out[4]);
+void oracle_im2col(const float *im, int channels, int height, int width, int ksize, int pad,
+                   int stride, float *col);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
