@@ -1,0 +1,342 @@
+"""Benchmark of the ugemm GB300 SGEMM backend.
+
+One step = one SGEMM C = 1.5*A*B + 0.5*C at M=N=K=8192, FP32 row-major, NN,
+inputs U[-1,1) (seeded, resident in HBM; each operand is 256 MiB, larger than
+the 129 MB L2, so no explicit flush between steps).  The headline `value` is
+the split-precision tensor-core form (BF16x6 on tcgen05) in TFLOPS
+(2*M*N*K per step); the plain FP32 SIMT form, both forms' normwise error
+against an FP64 GEMM on the GPU, the end-to-end number through the
+reference-facing host-pointer API (sgemm_cuda, pinned host buffers, copies
+inside the timed region) and the CPU baseline (the reference's AVX256 SGEMM,
+restated portably, on all host cores) go in the same JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) each rank runs an independent replica (the GEMM is
+not sharded: the spec path is one GPU); value = all ranks' flops / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TFLOPS @8192³: split-TC vs plain FP32 SIMT at equal FP64 err; grouped TFLOPS"
+SEED = 20261205
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(steps: int = 1):
+    """The reference's AVX256 SGEMM (restated portably in oracle/) on all host
+    cores, on a bounded row band of the 8192^3 NN problem."""
+    import numpy as np
+
+    import oracle
+    n = 8192
+    rows = int(os.environ.get("UGEMM_CPU_ROWS", "512"))
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(SEED)
+    A = rng.uniform(-1, 1, (rows, n)).astype(np.float32)
+    B = rng.uniform(-1, 1, (n, n)).astype(np.float32)
+    C = rng.uniform(-1, 1, (rows, n)).astype(np.float32)
+    oracle.load()
+    times = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        oracle.sgemm_avx256_mt(threads, "N", "N", rows, n, n, 1.5, A, B, 0.5, C)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    tflops = 2.0 * rows * n * n / t / 1e12
+    return {"value": round(tflops, 5), "unit": "TFLOPS", "cores": threads, "kind": "port",
+            "sample": f"rows 0..{rows - 1} of the 8192x8192x8192 NN problem (alpha=1.5, beta=0.5), "
+                      f"median of {len(times)} runs, {threads} threads, oracle AVX256 port",
+            "seconds_per_run": round(t, 4)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    for _ in range(min(args.warmup, 1)):
+        cpu_sample(1)
+    base = cpu_sample(steps)
+    line = {"metric": METRIC, "value": base["value"], "unit": "TFLOPS", "impl": "reference",
+            "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic U[-1,1) (seeded)",
+            "config": {"workload": "sgemm 8192x8192x8192 NN alpha=1.5 beta=0.5 (row band sample)",
+                       "model": "sgemm", "global_batch": 1, "seq_len": 0, "parallelism": "none"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "TFLOPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=8192)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import ugemm_gb300 as ug
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ug.build()
+    ug.load()
+
+    n = args.size
+    M = N = K = n
+    alpha, beta = 1.5, 0.5
+    flops = 2.0 * M * N * K
+    gen = torch.Generator(device="cuda").manual_seed(SEED + rank)
+    A = torch.rand((M, K), device="cuda", generator=gen) * 2 - 1
+    B = torch.rand((K, N), device="cuda", generator=gen) * 2 - 1
+    C0 = torch.rand((M, N), device="cuda", generator=gen) * 2 - 1
+    C = C0.clone()
+    stream = torch.cuda.current_stream()
+
+    def step(prec):
+        ug.sgemm_dev("N", "N", M, N, K, alpha, A, K, B, N, beta, C, N, precision=prec,
+                     stream=stream)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def timed(prec, steps, warmup):
+        for _ in range(max(warmup, 3)):
+            step(prec)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
+
+    # --- accuracy of each form against an FP64 GEMM of the same inputs
+    ref = None
+
+    def form_error(prec):
+        nonlocal ref
+        if ref is None:
+            ref = alpha * (A.double() @ B.double()) + beta * C0.double()
+        out = C0.clone()
+        ug.sgemm_dev("N", "N", M, N, K, alpha, A, K, B, N, beta, out, N, precision=prec,
+                     stream=stream)
+        torch.cuda.synchronize()
+        return float(torch.linalg.norm(out.double() - ref) / torch.linalg.norm(ref))
+
+    err_split = form_error("bf16x6")
+    err_simt = form_error("simt")
+    del ref
+    torch.cuda.empty_cache()
+
+    # --- headline: split-precision tensor-core form, device-resident inputs
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms_split = timed("bf16x6", args.steps, args.warmup)
+    clocks = sampler.stop()
+    ms_simt = timed("simt", max(2, args.steps // 2), 3)
+
+    # --- per-kernel attribution with CUDA events on the launching stream
+    ug.profile_enable(True)
+    for _ in range(3):
+        step("bf16x6")
+    prof = ug.profile_collect()
+    ug.profile_enable(False)
+    gemm_ms = prof["split_gemm"][0] / max(1, prof["split_gemm"][1])
+    prep_ms = prof["split_prepass"][0] / max(1, prof["split_prepass"][1])
+    launches_per_step = sum(v[1] for v in prof.values()) / 3.0
+
+    # --- end to end through the reference-facing host API (sgemm_cuda)
+    hA = A.cpu().pin_memory()
+    hB = B.cpu().pin_memory()
+    hC = C0.cpu().pin_memory()
+    size = (M * K + K * N + M * N) * 4 + ug.workspace_bytes("N", "N", M, N, K, K, N, "bf16x6")
+    lib = ug.load()
+    lib.sgemm_cuda_init(0, local, size + (64 << 20))
+    ug._check(lib.ugemm_last_error())
+    lib.sgemm_cuda_set_precision(ug.PREC_BF16X6)
+    e2e_steps = max(2, args.steps // 2)
+
+    def e2e_call():
+        ug._check(lib.sgemm_cuda_status(b"N", b"N", M, N, K, alpha, hA.data_ptr(), hB.data_ptr(),
+                                        beta, hC.data_ptr()))
+
+    for _ in range(2):
+        e2e_call()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_call()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    lib.sgemm_cuda_finish()
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    pk, pk_kind = peaks()
+    tflops_split = flops / (ms_split * 1e-3) / 1e12
+    tflops_simt = flops / (ms_simt * 1e-3) / 1e12
+    achieved = flops / (gemm_ms * 1e-3) / 1e12
+    peak_split = pk["bf16_tflops"] / 6.0
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "split_tc_traffic.json")) as f:
+            traffic = json.load(f).get("bytes_per_launch_8192")
+    except Exception:
+        pass
+
+    line = {
+        "metric": METRIC,
+        "value": round(tflops_split * world, 3),
+        "unit": "TFLOPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_split, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (bf16x6 split on tcgen05, FP32 accumulate)",
+        "data": "synthetic U[-1,1) (seeded, torch.Generator on device)",
+        "config": {"workload": f"sgemm {n}x{n}x{n} NN alpha=1.5 beta=0.5 row-major",
+                   "model": "sgemm", "global_batch": 1, "seq_len": 0,
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
+        "forms": {
+            "split_bf16x6": {"tflops": round(tflops_split, 3), "normwise_err_fp64": err_split},
+            "simt_fp32": {"tflops": round(tflops_simt, 3), "normwise_err_fp64": err_simt,
+                          "frac_of_fp32_peak_nominal": round(tflops_simt / fp32_peak, 4),
+                          "fp32_peak_nominal_tflops": round(fp32_peak, 2)},
+            "split_over_simt": round(tflops_split / tflops_simt, 3),
+            "split_err_over_simt_err": round(err_split / err_simt, 4),
+            "split_prepass_ms": round(prep_ms, 4), "split_gemm_ms": round(gemm_ms, 4),
+        },
+        "roofline": {"bound": "tensor", "achieved": round(achieved, 3),
+                     "peak": round(peak_split, 3), "unit": "TFLOP/s",
+                     "frac": round(achieved / peak_split, 4), "traffic": traffic,
+                     "kernel": "split_tc_kernel<3,256> (BF16x6)",
+                     "peak_basis": f"bf16_tflops ({pk_kind} cuBLAS burst {pk['bf16_tflops']}) / 6 "
+                                   "piece products; achieved = 2MNK / kernel time"},
+        "e2e": {"value": round(flops / e2e_s / 1e12 * world, 3), "unit": "TFLOPS",
+                "h2d_bytes_per_step": 3 * M * N * 4, "d2h_bytes_per_step": M * N * 4,
+                "api": "sgemm_cuda (compat, host pointers, pinned)"},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(3)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,144 @@
+/*
+ * sgemm_cuda.h -- GB300 (sm_103a) SGEMM backend for ugemm: C ABI of
+ * libugemm_cuda.so.
+ *
+ * Drop-in for the reference's GPU entry point (sgemm_ocl2.h:158-224, same
+ * API in sgemm_ocl.h:606-665 and sgemm_ocl1.h:159-252) and for its CPU GEMM
+ * signature (ugemm.h:287-301, the `uut` pointer of check_sgemm.c:96-103).
+ * All matrices are FP32.  Row-major unless a `major` argument says 'C'.
+ *
+ * Semantics kept from the reference:
+ *   - C = alpha * op(A) * op(B) + beta * C, op(X) = X ('N') or X^T ('T');
+ *   - sgemm_cuda: tight leading dimensions; ta == 'T' means A is stored K x M,
+ *     tb == 'T' means B is stored N x K (sgemm_ocl2.h:180-199);
+ *   - beta == 0 means C is not read, so NaNs in C do not propagate
+ *     (sgemm_ocl2.h:86-88, :177);
+ *   - one process-wide context for the compat API, set up by *_init and torn
+ *     down by *_finish (sgemm_ocl2.h:133-165, :220-224).
+ * Added: status codes instead of silent failure, device-pointer and stream
+ * entry points, split-precision tensor-core forms, the adjoint, grouped GEMM.
+ */
+#ifndef UGEMM_SGEMM_CUDA_H
+#define UGEMM_SGEMM_CUDA_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define UGEMM_API __attribute__((visibility("default")))
+#else
+#define UGEMM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  UGEMM_OK = 0,
+  UGEMM_ERR_ARG = 1,              /* bad transpose flag, size, leading dimension or pointer */
+  UGEMM_ERR_ALLOC = 2,            /* device or host allocation failed */
+  UGEMM_ERR_ARENA_TOO_SMALL = 3,  /* the init-time arena cannot hold this call */
+  UGEMM_ERR_CUDA = 4,             /* a CUDA runtime/driver call failed */
+  UGEMM_ERR_TIMEOUT = 5,          /* a kernel's bounded wait gave up (pipeline fault) */
+  UGEMM_ERR_NOT_INIT = 6,         /* compat call before sgemm_cuda_init */
+  UGEMM_ERR_UNSUPPORTED = 7,      /* no sm_103a device, or a form not available */
+} ugemm_status;
+
+/* Arithmetic form of a GEMM. */
+typedef enum {
+  UGEMM_PREC_AUTO = 0,   /* split-precision tensor cores when the problem is large enough */
+  UGEMM_PREC_SIMT = 1,   /* plain FP32 FMA on the CUDA cores */
+  UGEMM_PREC_BF16X6 = 2, /* 3 bf16 pieces per operand, 6 piece products (tcgen05) */
+  UGEMM_PREC_BF16X9 = 3, /* 3 bf16 pieces per operand, all 9 piece products (tcgen05) */
+  UGEMM_PREC_BF16X3 = 4, /* 2 bf16 pieces, 3 products: ~16-bit accuracy, for error studies */
+} ugemm_precision;
+
+/* ------------------------------------------------------------------ */
+/* Compat API: mirrors sgemm_ocl_init / sgemm_ocl / sgemm_ocl_finish.   */
+/* ------------------------------------------------------------------ */
+
+/* sgemm_ocl2.h:158 (sgemm_ocl_init).  `platform` is ignored (there is one
+ * CUDA platform); `device` selects the CUDA device; `size` is the byte size of
+ * the device arena that holds A, B, C and the call's scratch, as the
+ * reference's single OpenCL buffer does (sgemm_test.c:29 passes
+ * (M*K + K*N + M*N) * 10 * sizeof(float)).  Errors are kept in the last-error
+ * slot (ugemm_last_error). */
+UGEMM_API void sgemm_cuda_init(int platform, int device, size_t size);
+
+/* sgemm_ocl2.h:166 (sgemm_ocl).  Host pointers; synchronous; copies A, B
+ * (and C when beta != 0) to the device, runs the GEMM in the form chosen by
+ * sgemm_cuda_set_precision (default UGEMM_PREC_AUTO) and copies C back. */
+UGEMM_API void sgemm_cuda(char ta, char tb, int m, int n, int k, float alpha, float *a, float *b,
+                float beta, float *c);
+
+/* sgemm_ocl2.h:220 (sgemm_ocl_finish): frees the arena and the context. */
+UGEMM_API void sgemm_cuda_finish(void);
+
+/* Status-returning variant of sgemm_cuda (the compat call stores the same
+ * status in the last-error slot). */
+UGEMM_API int sgemm_cuda_status(char ta, char tb, int m, int n, int k, float alpha, const float *a,
+                      const float *b, float beta, float *c);
+
+/* Form used by sgemm_cuda / ugemm_sgemm (a ugemm_precision value). */
+UGEMM_API int sgemm_cuda_set_precision(int precision);
+
+/* Last status of a void entry point on this thread, and its message. */
+UGEMM_API int ugemm_last_error(void);
+UGEMM_API const char *ugemm_last_error_message(void);
+UGEMM_API const char *ugemm_status_string(int status);
+
+/* ------------------------------------------------------------------ */
+/* BLAS-style host API: the signature of ugemm.h:287 (sgemm_cpu) and of */
+/* the uut pointer in check_sgemm.c:96-103; works with or without init. */
+/* ------------------------------------------------------------------ */
+UGEMM_API void ugemm_sgemm(char major, char transa, char transb, int M, int N, int K, float alpha,
+                 const float *A, int lda, const float *B, int ldb, float beta, float *C,
+                 int ldc);
+UGEMM_API int ugemm_sgemm_host(char major, char transa, char transb, int M, int N, int K, float alpha,
+                     const float *A, int lda, const float *B, int ldb, float beta, float *C,
+                     int ldc, int precision);
+
+/* ------------------------------------------------------------------ */
+/* Device-pointer, stream-ordered API (no reference counterpart: the     */
+/* reference only has host pointers).  `stream` is a cudaStream_t (NULL */
+/* = legacy default stream).  Scratch comes from a library-owned device */
+/* workspace that grows on demand; reserve it with                      */
+/* ugemm_reserve_workspace before capturing these calls in a CUDA graph. */
+/* ------------------------------------------------------------------ */
+UGEMM_API int ugemm_sgemm_dev(char major, char transa, char transb, int M, int N, int K, float alpha,
+                    const float *A, int lda, const float *B, int ldb, float beta, float *C,
+                    int ldc, int precision, void *stream);
+
+/* Scratch bytes ugemm_sgemm_dev needs for this call (0 for most SIMT calls). */
+UGEMM_API size_t ugemm_workspace_bytes(char major, char transa, char transb, int M, int N, int K,
+                             int lda, int ldb, int precision);
+/* Grow the current device's workspace to at least `bytes`. */
+UGEMM_API int ugemm_reserve_workspace(size_t bytes);
+
+/* Adjoint of C = alpha*op(A)*op(B) + beta*C (spec differentiation form;
+ * no reference counterpart).  Given dC (M x N, row-major, lddc), writes
+ *   dA = alpha * dC * op(B)^T  (stored like A: M x K if transa=='N', else K x M)
+ *   dB = alpha * op(A)^T * dC  (stored like B: K x N if transb=='N', else N x K)
+ * as dX = grad + beta_x * dX (beta_x == 0: dX is not read).  dA or dB may be
+ * NULL to skip it.  Device pointers, row-major. */
+UGEMM_API int ugemm_sgemm_backward(char transa, char transb, int M, int N, int K, float alpha,
+                         const float *A, int lda, const float *B, int ldb, const float *dC,
+                         int lddc, float beta_a, float *dA, int ldda, float beta_b, float *dB,
+                         int lddb, int precision, void *stream);
+
+/* Device information: SM count and compute capability of the current device. */
+UGEMM_API int ugemm_device_info(int *sm_count, int *cc_major, int *cc_minor);
+
+/* Per-kernel timing for benchmarks (no reference counterpart; the reference's
+ * oclTime at ocl.h:344-352 is never enabled).  While enabled, each library
+ * kernel launch is bracketed by CUDA events on its own stream.  collect()
+ * synchronises, returns the summed milliseconds and launch counts per kind
+ * (0 SIMT GEMM, 1 split pre-pass, 2 split tcgen05 GEMM, 3 auxiliary, 4 grouped
+ * GEMM) and clears the record. */
+UGEMM_API int ugemm_profile_enable(int on);
+UGEMM_API int ugemm_profile_collect(double *ms_per_kind, int *launches_per_kind, int nkinds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UGEMM_SGEMM_CUDA_H */

@@ -1,0 +1,89 @@
+"""The C-ABI library builds, loads without a GPU and exports every symbol the
+public headers declare; host-side argument checks need no GPU."""
+import ctypes
+import os
+import re
+import shutil
+
+import pytest
+
+import ugemm_gb300 as ug
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for fn in sorted(os.listdir(inc)):
+        if fn.endswith(".h"):
+            text = open(os.path.join(inc, fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names += re.findall(r"^\s*(?:UGEMM_API\s+)?(?:const\s+)?[a-z_]+\s*\**\s*([a-z_][a-z0-9_]*)\s*\(", text,
+                                re.M)
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(ug.LIB_PATH):
+        if shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+            pytest.skip("nvcc not available to build the library")
+        ug.build()
+    return ug.load()
+
+
+def test_exports_every_header_symbol(lib):
+    names = header_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(ug.EXPORTS) <= set(names)
+
+
+def test_only_c_abi_symbols_are_exported(lib):
+    # Internal C++ symbols are hidden; no torch types leak through the ABI.
+    import subprocess
+    out = subprocess.run(["nm", "-D", "--defined-only", ug.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    ours = {n for n in exported if n.startswith(("ugemm_", "sgemm_"))}
+    assert set(header_functions()) <= ours
+
+
+def test_status_strings(lib):
+    assert lib.ugemm_status_string(0) == b"ok"
+    assert b"argument" in lib.ugemm_status_string(ug.ERR_ARG)
+    assert lib.ugemm_status_string(99) == b"unknown status"
+
+
+def test_argument_checks_need_no_gpu(lib):
+    f = lib.ugemm_sgemm_dev
+    # bad transpose flag
+    assert f(b"R", b"X", b"N", 4, 4, 4, 1.0, 16, 4, 16, 4, 0.0, 16, 4, 0, None) == ug.ERR_ARG
+    # bad major
+    assert f(b"Q", b"N", b"N", 4, 4, 4, 1.0, 16, 4, 16, 4, 0.0, 16, 4, 0, None) == ug.ERR_ARG
+    # negative size
+    assert f(b"R", b"N", b"N", -1, 4, 4, 1.0, 16, 4, 16, 4, 0.0, 16, 4, 0, None) == ug.ERR_ARG
+    # lda < K for a row-major 'N' A
+    assert f(b"R", b"N", b"N", 4, 4, 8, 1.0, 16, 4, 16, 4, 0.0, 16, 4, 0, None) == ug.ERR_ARG
+    # ldc < N
+    assert f(b"R", b"N", b"N", 4, 8, 4, 1.0, 16, 4, 16, 8, 0.0, 16, 4, 0, None) == ug.ERR_ARG
+    # NULL C
+    assert f(b"R", b"N", b"N", 4, 4, 4, 1.0, 16, 4, 16, 4, 0.0, None, 4, 0, None) == ug.ERR_ARG
+    assert b"leading" in lib.ugemm_last_error_message() or lib.ugemm_last_error() == ug.ERR_ARG
+    # empty problems are a no-op before any device work
+    assert f(b"R", b"N", b"N", 0, 4, 4, 1.0, None, 4, None, 4, 0.0, None, 4, 0, None) == ug.OK
+
+
+def test_compat_requires_init(lib):
+    assert lib.sgemm_cuda_status(b"N", b"N", 2, 2, 2, 1.0, None, None, 0.0, None) == ug.ERR_NOT_INIT
+
+
+def test_workspace_query_is_host_only(lib):
+    # split-precision form: 3 bf16 pieces of A (M x Kp) and B (N x Kp)
+    n = ug.workspace_bytes("N", "N", 1024, 1024, 1024, 1024, 1024, "bf16x6")
+    assert n == 2 * 3 * 1024 * 1024 * 2
+    assert ug.workspace_bytes("N", "N", 1024, 1024, 1024, 1024, 1024, "simt") == 0
+    # unaligned lda forces a packed copy in the SIMT form
+    assert ug.workspace_bytes("N", "N", 64, 64, 63, 63, 64, "simt") > 0

@@ -1,0 +1,252 @@
+"""ugemm_gb300 -- Python host mirror of the GB300 SGEMM backend for ugemm.
+
+The product is ``libugemm_cuda.so`` (C ABI in ``include/sgemm_cuda.h``); this
+module loads it with ctypes and mirrors the reference's entry points with the
+same names and argument meaning:
+
+* ``sgemm_cuda_init(platform, device, size)`` / ``sgemm_cuda(ta, tb, m, n, k,
+  alpha, a, b, beta, c)`` / ``sgemm_cuda_finish()`` -- the reference's
+  ``sgemm_ocl_init`` / ``sgemm_ocl`` / ``sgemm_ocl_finish`` (sgemm_ocl2.h:158,
+  166, 220) on numpy float32 host arrays;
+* ``ugemm_sgemm(major, transa, transb, M, N, K, alpha, A, lda, B, ldb, beta,
+  C, ldc)`` -- the signature of ``sgemm_cpu`` (ugemm.h:287);
+* ``sgemm_dev`` / ``sgemm_backward`` -- device-pointer forms on torch CUDA
+  tensors (torch is used only for device memory and streams).
+
+There is no CPU fallback: if the CUDA library is missing or cannot run, every
+call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libugemm_cuda.so")
+
+OK = 0
+ERR_ARG = 1
+ERR_ALLOC = 2
+ERR_ARENA_TOO_SMALL = 3
+ERR_CUDA = 4
+ERR_TIMEOUT = 5
+ERR_NOT_INIT = 6
+ERR_UNSUPPORTED = 7
+
+PREC_AUTO = 0
+PREC_SIMT = 1
+PREC_BF16X6 = 2
+PREC_BF16X9 = 3
+PREC_BF16X3 = 4
+PRECISIONS = {"auto": PREC_AUTO, "simt": PREC_SIMT, "bf16x6": PREC_BF16X6, "bf16x9": PREC_BF16X9,
+              "bf16x3": PREC_BF16X3}
+
+# Every symbol include/sgemm_cuda.h declares.
+EXPORTS = (
+    "sgemm_cuda_init", "sgemm_cuda", "sgemm_cuda_finish", "sgemm_cuda_status",
+    "sgemm_cuda_set_precision", "ugemm_last_error", "ugemm_last_error_message",
+    "ugemm_status_string", "ugemm_sgemm", "ugemm_sgemm_host", "ugemm_sgemm_dev",
+    "ugemm_workspace_bytes", "ugemm_reserve_workspace", "ugemm_sgemm_backward",
+    "ugemm_device_info", "ugemm_profile_enable", "ugemm_profile_collect",
+)
+PROF_KINDS = ("simt", "split_prepass", "split_gemm", "aux", "grouped")
+
+
+class UgemmError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"ugemm status {status}: {msg}")
+
+
+_lib = None
+_c = ctypes.c_char
+_i = ctypes.c_int
+_f = ctypes.c_float
+_p = ctypes.c_void_p
+_sz = ctypes.c_size_t
+
+
+def build(verbose: bool = False) -> str:
+    from . import build as _b
+    return _b.build(verbose=verbose)
+
+
+def load() -> ctypes.CDLL:
+    """Load libugemm_cuda.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise UgemmError(ERR_UNSUPPORTED, f"{LIB_PATH} is missing: run __graft_entry__.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    gemm = [_c, _c, _c, _i, _i, _i, _f, _p, _i, _p, _i, _f, _p, _i]
+    lib.sgemm_cuda_init.argtypes = [_i, _i, _sz]
+    lib.sgemm_cuda_init.restype = None
+    lib.sgemm_cuda.argtypes = [_c, _c, _i, _i, _i, _f, _p, _p, _f, _p]
+    lib.sgemm_cuda.restype = None
+    lib.sgemm_cuda_status.argtypes = [_c, _c, _i, _i, _i, _f, _p, _p, _f, _p]
+    lib.sgemm_cuda_status.restype = _i
+    lib.sgemm_cuda_finish.argtypes = []
+    lib.sgemm_cuda_finish.restype = None
+    lib.sgemm_cuda_set_precision.argtypes = [_i]
+    lib.sgemm_cuda_set_precision.restype = _i
+    lib.ugemm_last_error.argtypes = []
+    lib.ugemm_last_error.restype = _i
+    lib.ugemm_last_error_message.argtypes = []
+    lib.ugemm_last_error_message.restype = ctypes.c_char_p
+    lib.ugemm_status_string.argtypes = [_i]
+    lib.ugemm_status_string.restype = ctypes.c_char_p
+    lib.ugemm_sgemm.argtypes = gemm
+    lib.ugemm_sgemm.restype = None
+    lib.ugemm_sgemm_host.argtypes = gemm + [_i]
+    lib.ugemm_sgemm_host.restype = _i
+    lib.ugemm_sgemm_dev.argtypes = gemm + [_i, _p]
+    lib.ugemm_sgemm_dev.restype = _i
+    lib.ugemm_workspace_bytes.argtypes = [_c, _c, _c, _i, _i, _i, _i, _i, _i]
+    lib.ugemm_workspace_bytes.restype = _sz
+    lib.ugemm_reserve_workspace.argtypes = [_sz]
+    lib.ugemm_reserve_workspace.restype = _i
+    lib.ugemm_sgemm_backward.argtypes = [_c, _c, _i, _i, _i, _f, _p, _i, _p, _i, _p, _i, _f, _p, _i,
+                                         _f, _p, _i, _i, _p]
+    lib.ugemm_sgemm_backward.restype = _i
+    lib.ugemm_device_info.argtypes = [ctypes.POINTER(_i)] * 3
+    lib.ugemm_device_info.restype = _i
+    lib.ugemm_profile_enable.argtypes = [_i]
+    lib.ugemm_profile_enable.restype = _i
+    lib.ugemm_profile_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i), _i]
+    lib.ugemm_profile_collect.restype = _i
+    _lib = lib
+    return lib
+
+
+def _check(status: int) -> None:
+    if status != OK:
+        msg = load().ugemm_last_error_message().decode(errors="replace")
+        raise UgemmError(status, msg)
+
+
+def _prec(p) -> int:
+    return PRECISIONS[p] if isinstance(p, str) else int(p)
+
+
+def _host_ptr(a: np.ndarray, writable: bool = False) -> int:
+    if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"]:
+        raise UgemmError(ERR_ARG, "host arrays must be C-contiguous float32")
+    if writable and not a.flags["WRITEABLE"]:
+        raise UgemmError(ERR_ARG, "C must be writable")
+    return a.ctypes.data
+
+
+# --------------------------------------------------------------------------
+# Reference-named compat API (sgemm_ocl2.h:158-224)
+# --------------------------------------------------------------------------
+def sgemm_cuda_init(platform: int = 0, device: int = 0, size: int = 0) -> None:
+    lib = load()
+    lib.sgemm_cuda_init(platform, device, size)
+    _check(lib.ugemm_last_error())
+
+
+def sgemm_cuda(ta: str, tb: str, m: int, n: int, k: int, alpha: float, a: np.ndarray,
+               b: np.ndarray, beta: float, c: np.ndarray) -> None:
+    """C = alpha*op(A)*op(B) + beta*C on host arrays (tight leading dims)."""
+    lib = load()
+    _check(lib.sgemm_cuda_status(ta.encode(), tb.encode(), m, n, k, alpha, _host_ptr(a),
+                                 _host_ptr(b), beta, _host_ptr(c, True)))
+
+
+def sgemm_cuda_finish() -> None:
+    load().sgemm_cuda_finish()
+
+
+def set_precision(precision) -> None:
+    _check(load().sgemm_cuda_set_precision(_prec(precision)))
+
+
+def ugemm_sgemm(major: str, transa: str, transb: str, M: int, N: int, K: int, alpha: float,
+                A: np.ndarray, lda: int, B: np.ndarray, ldb: int, beta: float, C: np.ndarray,
+                ldc: int, precision="auto") -> None:
+    """BLAS-style host GEMM with the sgemm_cpu signature (ugemm.h:287)."""
+    lib = load()
+    _check(lib.ugemm_sgemm_host(major.encode(), transa.encode(), transb.encode(), M, N, K, alpha,
+                                _host_ptr(A), lda, _host_ptr(B), ldb, beta, _host_ptr(C, True),
+                                ldc, _prec(precision)))
+
+
+# --------------------------------------------------------------------------
+# Device-pointer API on torch tensors
+# --------------------------------------------------------------------------
+def _stream_ptr(stream) -> int:
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return stream.cuda_stream
+
+
+def sgemm_dev(ta: str, tb: str, M: int, N: int, K: int, alpha: float, A, lda: int, B, ldb: int,
+              beta: float, C, ldc: int, precision="auto", stream=None, major: str = "R") -> None:
+    """Row-major (or 'C') GEMM on device memory (torch CUDA tensors or ints)."""
+    lib = load()
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_sgemm_dev(major.encode(), ta.encode(), tb.encode(), M, N, K, alpha, ptr(A),
+                               lda, ptr(B), ldb, beta, ptr(C), ldc, _prec(precision),
+                               _stream_ptr(stream)))
+
+
+def gemm(A, B, C=None, *, ta: str = "N", tb: str = "N", alpha: float = 1.0, beta: float = 0.0,
+         precision="auto", stream=None):
+    """C = alpha*op(A)*op(B) + beta*C on 2-D row-major float32 CUDA tensors."""
+    import torch
+    M = A.shape[0] if ta == "N" else A.shape[1]
+    K = A.shape[1] if ta == "N" else A.shape[0]
+    N = B.shape[1] if tb == "N" else B.shape[0]
+    if C is None:
+        C = torch.empty((M, N), dtype=torch.float32, device=A.device)
+    for t in (A, B, C):
+        if t.dtype != torch.float32 or t.stride(1) != 1:
+            raise UgemmError(ERR_ARG, "tensors must be float32 with unit column stride")
+    sgemm_dev(ta, tb, M, N, K, alpha, A, A.stride(0), B, B.stride(0), beta, C, C.stride(0),
+              precision, stream)
+    return C
+
+
+def sgemm_backward(ta: str, tb: str, M: int, N: int, K: int, alpha: float, A, lda: int, B,
+                   ldb: int, dC, lddc: int, beta_a: float, dA, ldda: int, beta_b: float, dB,
+                   lddb: int, precision="auto", stream=None) -> None:
+    """dA = alpha*dC*op(B)^T (+beta_a*dA), dB = alpha*op(A)^T*dC (+beta_b*dB)."""
+    lib = load()
+    ptr = (lambda t: 0 if t is None else (t if isinstance(t, int) else t.data_ptr()))
+    _check(lib.ugemm_sgemm_backward(ta.encode(), tb.encode(), M, N, K, alpha, ptr(A), lda, ptr(B),
+                                    ldb, ptr(dC), lddc, beta_a, ptr(dA), ldda, beta_b, ptr(dB),
+                                    lddb, _prec(precision), _stream_ptr(stream)))
+
+
+def workspace_bytes(ta: str, tb: str, M: int, N: int, K: int, lda: int, ldb: int,
+                    precision="auto", major: str = "R") -> int:
+    return int(load().ugemm_workspace_bytes(major.encode(), ta.encode(), tb.encode(), M, N, K, lda,
+                                            ldb, _prec(precision)))
+
+
+def reserve_workspace(nbytes: int) -> None:
+    _check(load().ugemm_reserve_workspace(nbytes))
+
+
+def device_info():
+    lib = load()
+    sm, ma, mi = _i(), _i(), _i()
+    _check(lib.ugemm_device_info(ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)))
+    return sm.value, ma.value, mi.value
+
+
+def profile_enable(on: bool = True) -> None:
+    _check(load().ugemm_profile_enable(1 if on else 0))
+
+
+def profile_collect() -> dict:
+    """{kind: (milliseconds, launches)} since the last collect (synchronises)."""
+    n = len(PROF_KINDS)
+    ms = (ctypes.c_double * n)()
+    cnt = (_i * n)()
+    _check(load().ugemm_profile_collect(ms, cnt, n))
+    return {k: (ms[i], cnt[i]) for i, k in enumerate(PROF_KINDS)}

@@ -1,0 +1,86 @@
+// internal.h -- declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/sgemm_cuda.h"
+
+namespace ugemm {
+
+// A row-major GEMM after argument normalisation (column-major calls are
+// rewritten as the transposed row-major problem before they get here):
+//   C[M x N] = alpha * op(A)[M x K] * op(B)[K x N] + beta * C
+// ta == 'N': A is M x K (lda >= K);  ta == 'T': A is K x M (lda >= M).
+// tb == 'N': B is K x N (ldb >= N);  tb == 'T': B is N x K (ldb >= K).
+// beta == 0 means C is written without being read.
+struct Gemm {
+  char ta, tb;
+  int M, N, K;
+  float alpha, beta;
+  const float* A;
+  int lda;
+  const float* B;
+  int ldb;
+  float* C;
+  int ldc;
+};
+
+// Device scratch handed to a launcher.  `bytes` is what is available at `ptr`.
+struct Scratch {
+  void* ptr;
+  size_t bytes;
+};
+
+// Tile configurations of the SIMT kernel (rows x cols of C per CTA).
+enum SimtTile : int { kSimt128x128 = 0, kSimt64x64 = 1, kSimtTileCount = 2 };
+
+// Split-precision tensor-core variants.
+struct SplitPlan {
+  int pieces;    // bf16 pieces per FP32 operand (2 or 3)
+  int products;  // number of piece products accumulated (3, 6 or 9)
+  int block_n;   // CTA tile width (128 or 256)
+};
+
+// --- tensor maps -------------------------------------------------------
+bool encode_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, int elem_bytes,
+                    const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                    uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz);
+bool encode_tmap_3d(CUtensorMap* map, CUtensorMapDataType dtype, int elem_bytes,
+                    const void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t stride1,
+                    uint64_t stride2, uint32_t b0, uint32_t b1, uint32_t b2,
+                    CUtensorMapSwizzle swz);
+
+// --- SIMT path ---------------------------------------------------------
+size_t simt_scratch_bytes(const Gemm& g);
+ugemm_status simt_launch(const Gemm& g, int tile, Scratch ws, int* dev_err, cudaStream_t st);
+int simt_pick_tile(const Gemm& g);
+
+// --- split-precision tensor-core path ----------------------------------
+size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p);
+ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* dev_err,
+                          cudaStream_t st);
+SplitPlan split_plan_for(int precision, const Gemm& g);
+
+// --- small helpers -----------------------------------------------------
+ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st);  // C = beta*C (or 0)
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// Per-thread last error, shared by the void compat entry points.
+void set_last_error(ugemm_status s, const std::string& msg);
+
+}  // namespace ugemm
+
+namespace ugemm {
+// Optional per-kernel timing (CUDA events on the launching stream), enabled by
+// ugemm_profile_enable; used by the benchmark to attribute time to kernels.
+enum ProfKind : int { kProfSimt = 0, kProfSplitPrep = 1, kProfSplitGemm = 2, kProfAux = 3,
+                      kProfGrouped = 4, kProfKinds = 5 };
+void prof_begin(cudaStream_t st);
+void prof_end(cudaStream_t st, int kind);
+}  // namespace ugemm

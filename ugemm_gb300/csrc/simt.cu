@@ -1,0 +1,355 @@
+// simt.cu -- plain FP32 SIMT SGEMM for sm_103a (the "plain" form).
+//
+// Replaces the reference's OpenCL gemm_rnn (sgemm_ocl2.h:17-90: 16x16 tile,
+// one output per work-item, two local-memory loads per FMA) and its separate
+// transpose pass (sgemm_ocl2.h:95-128, :180-199).  Here:
+//   * one CTA computes a BM x BN tile of C; 8 consumer warps (16 x 16 threads)
+//     each hold a TM x TN register block; a ninth warp is the TMA producer;
+//   * A and B k-slices (BK = 16) are staged by TMA into a 4-deep shared-memory
+//     ring guarded by mbarriers; k-contiguous tiles use the 64-byte swizzle
+//     so the float4 fragment reads are bank-conflict free;
+//   * transposed operands are handled by the tile layout (an m- or
+//     n-contiguous tile) -- no transpose kernel, no extra HBM pass;
+//   * ragged edges: TMA zero-fills out-of-range rows/columns/k, the epilogue
+//     guards its stores; alpha/beta are fused into the epilogue and C is not
+//     read when beta == 0 (sgemm_ocl2.h:86-88).
+// Operands whose base or leading dimension break TMA's 16-byte rules are
+// first copied into an aligned scratch buffer (simt_scratch_bytes).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "internal.h"
+#include "ptx.cuh"
+
+namespace ugemm {
+namespace {
+
+constexpr int kBK = 16;            // k depth of one pipeline stage
+constexpr int kStages = 4;         // TMA ring depth
+constexpr int kConsumerWarps = 8;  // 16 x 16 compute threads
+constexpr int kThreads = (kConsumerWarps + 1) * 32;
+constexpr int kRaster = 8;         // rows of tiles per raster group (L2 reuse)
+
+template <int TM, int TN>
+struct SimtShape {
+  static constexpr int BM = 16 * TM;
+  static constexpr int BN = 16 * TN;
+  static constexpr int A_BYTES = BM * kBK * 4;
+  static constexpr int B_BYTES = BN * kBK * 4;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr size_t SMEM = 1024 + size_t(kStages) * STAGE_BYTES + 2 * kStages * 8;
+};
+
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+// Position of the 16-byte chunk `q` of row `r` in a 64-byte-row tile written
+// by TMA with CU_TENSOR_MAP_SWIZZLE_64B (address bits [4,6) ^= bits [7,9)).
+__device__ __forceinline__ int sw64_chunk(int r, int q) { return q ^ ((r >> 1) & 3); }
+
+// AK: op(A) rows are k-contiguous (ta == 'N').  BKM: op(B) columns are
+// k-contiguous (tb == 'T').
+template <int TM, int TN, bool AK, bool BKM>
+__global__ void __launch_bounds__(kThreads, 1)
+    simt_sgemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                      const __grid_constant__ CUtensorMap tmB, float* __restrict__ C, int M,
+                      int N, int K, int ldc, float alpha, float beta, int tiles_m, int tiles_n,
+                      int* err) {
+  using S = SimtShape<TM, TN>;
+  constexpr int BM = S::BM, BN = S::BN;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::STAGE_BYTES);
+  uint64_t* empty = full + kStages;
+
+  // Grouped raster: kRaster consecutive tile rows share their B columns in L2.
+  const int b = blockIdx.x;
+  const int per_group = kRaster * tiles_n;
+  const int first_m = (b / per_group) * kRaster;
+  const int group_rows = min(tiles_m - first_m, kRaster);
+  const int tile_m = first_m + (b % per_group) % group_rows;
+  const int tile_n = (b % per_group) / group_rows;
+  const int m0 = tile_m * BM, n0 = tile_n * BN;
+  const int nkt = (K + kBK - 1) / kBK;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  if (warp == kConsumerWarps) {  // ---------------- TMA producer warp
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      for (int kt = 0; kt < nkt; ++kt) {
+        const int s = kt % kStages;
+        const uint32_t ph = (kt / kStages) & 1;
+        if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) break;
+        uint8_t* sa = smem + s * S::STAGE_BYTES;
+        uint8_t* sb = sa + S::A_BYTES;
+        mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
+        if (AK) tma_load_2d(sa, &tmA, &full[s], kt * kBK, m0);
+        else    tma_load_2d(sa, &tmA, &full[s], m0, kt * kBK);
+        if (BKM) tma_load_2d(sb, &tmB, &full[s], kt * kBK, n0);
+        else     tma_load_2d(sb, &tmB, &full[s], n0, kt * kBK);
+      }
+    }
+    return;
+  }
+
+  // ---------------------------------------------------- consumer warps
+  const int ty = tid >> 4, tx = tid & 15;
+  float acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+
+  bool ok = true;
+  for (int kt = 0; kt < nkt; ++kt) {
+    const int s = kt % kStages;
+    const uint32_t ph = (kt / kStages) & 1;
+    if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) { ok = false; break; }
+    const float* As = reinterpret_cast<const float*>(smem + s * S::STAGE_BYTES);
+    const float* Bs = reinterpret_cast<const float*>(smem + s * S::STAGE_BYTES + S::A_BYTES);
+#pragma unroll
+    for (int q = 0; q < kBK / 4; ++q) {
+      float a[TM][4], bf[TN][4];
+      if (AK) {  // As[BM][16], 64-byte swizzled rows; thread rows ty + 16 i
+#pragma unroll
+        for (int i = 0; i < TM; ++i) {
+          const int r = ty + 16 * i;
+          const float4 v = *reinterpret_cast<const float4*>(As + r * kBK + 4 * sw64_chunk(r, q));
+          a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
+        }
+      } else {   // As[16][BM]; thread rows 64 g + 4 ty + {0..3}
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int g = 0; g < TM / 4; ++g) {
+            const float4 v =
+                *reinterpret_cast<const float4*>(As + (4 * q + kk) * BM + 64 * g + 4 * ty);
+            a[4 * g + 0][kk] = v.x; a[4 * g + 1][kk] = v.y;
+            a[4 * g + 2][kk] = v.z; a[4 * g + 3][kk] = v.w;
+          }
+      }
+      if (BKM) {  // Bs[BN][16], 64-byte swizzled rows; thread cols tx + 16 j
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+          const int c = tx + 16 * j;
+          const float4 v = *reinterpret_cast<const float4*>(Bs + c * kBK + 4 * sw64_chunk(c, q));
+          bf[j][0] = v.x; bf[j][1] = v.y; bf[j][2] = v.z; bf[j][3] = v.w;
+        }
+      } else {    // Bs[16][BN]; thread cols 64 g + 4 tx + {0..3}
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int g = 0; g < TN / 4; ++g) {
+            const float4 v =
+                *reinterpret_cast<const float4*>(Bs + (4 * q + kk) * BN + 64 * g + 4 * tx);
+            bf[4 * g + 0][kk] = v.x; bf[4 * g + 1][kk] = v.y;
+            bf[4 * g + 2][kk] = v.z; bf[4 * g + 3][kk] = v.w;
+          }
+      }
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i][kk], bf[j][kk], acc[i][j]);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+  if (!ok) return;
+
+  // ------------------------------------------------------------ epilogue
+  const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int row = m0 + (AK ? ty + 16 * i : 64 * (i / 4) + 4 * ty + (i % 4));
+    if (row >= M) continue;
+    float* crow = C + static_cast<size_t>(row) * ldc;
+    if (BKM) {
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const int col = n0 + tx + 16 * j;
+        if (col < N) {
+          float v = alpha * acc[i][j];
+          if (beta != 0.f) v += beta * crow[col];
+          crow[col] = v;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < TN / 4; ++g) {
+        const int col = n0 + 64 * g + 4 * tx;
+        if (vec && col + 3 < N) {
+          float4 v = make_float4(alpha * acc[i][4 * g], alpha * acc[i][4 * g + 1],
+                                 alpha * acc[i][4 * g + 2], alpha * acc[i][4 * g + 3]);
+          if (beta != 0.f) {
+            const float4 o = *reinterpret_cast<const float4*>(crow + col);
+            v.x += beta * o.x; v.y += beta * o.y; v.z += beta * o.z; v.w += beta * o.w;
+          }
+          *reinterpret_cast<float4*>(crow + col) = v;
+        } else {
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj)
+            if (col + jj < N) {
+              float v = alpha * acc[i][4 * g + jj];
+              if (beta != 0.f) v += beta * crow[col + jj];
+              crow[col + jj] = v;
+            }
+        }
+      }
+    }
+  }
+}
+
+// Copy a rows x cols row-major matrix into a dense buffer whose rows are
+// `ldd` floats (a multiple of 4) so that TMA can describe it.
+__global__ void pack_rows_kernel(const float* __restrict__ src, int lds, float* __restrict__ dst,
+                                 int ldd, int rows, int cols) {
+  const size_t total = static_cast<size_t>(rows) * ldd;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    const int r = static_cast<int>(i / ldd), c = static_cast<int>(i % ldd);
+    dst[i] = (c < cols) ? src[static_cast<size_t>(r) * lds + c] : 0.f;
+  }
+}
+
+__global__ void scale_kernel(float* __restrict__ C, int M, int N, int ldc, float beta) {
+  const size_t total = static_cast<size_t>(M) * N;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total;
+       i += size_t(gridDim.x) * blockDim.x) {
+    float* p = C + (i / N) * static_cast<size_t>(ldc) + (i % N);
+    *p = (beta == 0.f) ? 0.f : beta * *p;
+  }
+}
+
+bool tma_ok(const void* p, int ld) {
+  return (reinterpret_cast<uintptr_t>(p) & 15) == 0 && (ld % 4) == 0;
+}
+
+// Stored shape (rows, cols) of an operand.
+void stored_a(const Gemm& g, int& rows, int& cols) {
+  if (g.ta == 'N') { rows = g.M; cols = g.K; } else { rows = g.K; cols = g.M; }
+}
+void stored_b(const Gemm& g, int& rows, int& cols) {
+  if (g.tb == 'N') { rows = g.K; cols = g.N; } else { rows = g.N; cols = g.K; }
+}
+
+template <int TM, int TN, bool AK, bool BKM>
+ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, int ldb,
+                      int* dev_err, cudaStream_t st) {
+  using S = SimtShape<TM, TN>;
+  CUtensorMap ta, tb;
+  bool ok;
+  if (AK) ok = encode_tmap_2d(&ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, A, g.K, g.M, lda * 4ull,
+                              kBK, S::BM, CU_TENSOR_MAP_SWIZZLE_64B);
+  else    ok = encode_tmap_2d(&ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, A, g.M, g.K, lda * 4ull,
+                              S::BM, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!ok) return UGEMM_ERR_CUDA;
+  if (BKM) ok = encode_tmap_2d(&tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, B, g.K, g.N, ldb * 4ull,
+                               kBK, S::BN, CU_TENSOR_MAP_SWIZZLE_64B);
+  else     ok = encode_tmap_2d(&tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, B, g.N, g.K, ldb * 4ull,
+                               S::BN, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!ok) return UGEMM_ERR_CUDA;
+  auto kern = simt_sgemm_kernel<TM, TN, AK, BKM>;
+  static bool attr_set = false;  // per instantiation
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(S::SMEM)) != cudaSuccess)
+      return UGEMM_ERR_CUDA;
+    attr_set = true;
+  }
+  const int tiles_m = cdiv(g.M, S::BM), tiles_n = cdiv(g.N, S::BN);
+  prof_begin(st);
+  kern<<<tiles_m * tiles_n, kThreads, S::SMEM, st>>>(ta, tb, g.C, g.M, g.N, g.K, g.ldc, g.alpha,
+                                                      g.beta, tiles_m, tiles_n, dev_err);
+  prof_end(st, kProfSimt);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+template <int TM, int TN>
+ugemm_status launch_tile(const Gemm& g, const float* A, int lda, const float* B, int ldb,
+                         int* dev_err, cudaStream_t st) {
+  const bool ak = g.ta == 'N', bk = g.tb == 'T';
+  if (ak && !bk) return launch_t<TM, TN, true, false>(g, A, lda, B, ldb, dev_err, st);
+  if (ak && bk) return launch_t<TM, TN, true, true>(g, A, lda, B, ldb, dev_err, st);
+  if (!ak && !bk) return launch_t<TM, TN, false, false>(g, A, lda, B, ldb, dev_err, st);
+  return launch_t<TM, TN, false, true>(g, A, lda, B, ldb, dev_err, st);
+}
+
+}  // namespace
+
+size_t simt_scratch_bytes(const Gemm& g) {
+  size_t bytes = 0;
+  int r, c;
+  if (!tma_ok(g.A, g.lda)) { stored_a(g, r, c); bytes += align_up(size_t(r) * align_up(c, 4) * 4, 256); }
+  if (!tma_ok(g.B, g.ldb)) { stored_b(g, r, c); bytes += align_up(size_t(r) * align_up(c, 4) * 4, 256); }
+  return bytes;
+}
+
+int simt_pick_tile(const Gemm& g) {
+  int sms = 148;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long big = long(cdiv(g.M, 128)) * cdiv(g.N, 128);
+  return big >= 2L * sms ? kSimt128x128 : kSimt64x64;
+}
+
+ugemm_status simt_launch(const Gemm& g, int tile, Scratch ws, int* dev_err, cudaStream_t st) {
+  const float* A = g.A;
+  const float* B = g.B;
+  int lda = g.lda, ldb = g.ldb;
+  uint8_t* wp = static_cast<uint8_t*>(ws.ptr);
+  size_t used = 0;
+  int r, c;
+  if (!tma_ok(A, lda)) {
+    stored_a(g, r, c);
+    const int ld = static_cast<int>(align_up(c, 4));
+    const size_t need = align_up(size_t(r) * ld * 4, 256);
+    if (used + need > ws.bytes) return UGEMM_ERR_ARENA_TOO_SMALL;
+    float* dst = reinterpret_cast<float*>(wp + used);
+    prof_begin(st);
+    pack_rows_kernel<<<std::min<size_t>(4096, (size_t(r) * ld + 255) / 256), 256, 0, st>>>(
+        A, lda, dst, ld, r, c);
+    prof_end(st, kProfAux);
+    A = dst; lda = ld; used += need;
+  }
+  if (!tma_ok(B, ldb)) {
+    stored_b(g, r, c);
+    const int ld = static_cast<int>(align_up(c, 4));
+    const size_t need = align_up(size_t(r) * ld * 4, 256);
+    if (used + need > ws.bytes) return UGEMM_ERR_ARENA_TOO_SMALL;
+    float* dst = reinterpret_cast<float*>(wp + used);
+    prof_begin(st);
+    pack_rows_kernel<<<std::min<size_t>(4096, (size_t(r) * ld + 255) / 256), 256, 0, st>>>(
+        B, ldb, dst, ld, r, c);
+    prof_end(st, kProfAux);
+    B = dst; ldb = ld; used += need;
+  }
+  if (tile == kSimt64x64) return launch_tile<4, 4>(g, A, lda, B, ldb, dev_err, st);
+  return launch_tile<8, 8>(g, A, lda, B, ldb, dev_err, st);
+}
+
+ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st) {
+  if (g.M <= 0 || g.N <= 0 || g.beta == 1.f) return UGEMM_OK;
+  const size_t total = size_t(g.M) * g.N;
+  prof_begin(st);
+  scale_kernel<<<std::min<size_t>(4096, (total + 255) / 256), 256, 0, st>>>(g.C, g.M, g.N, g.ldc,
+                                                                            g.beta);
+  prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+}  // namespace ugemm
