@@ -69,8 +69,8 @@ _sz = ctypes.c_size_t
 
 
 def build(verbose: bool = False) -> str:
-    from . import build as _b
-    return _b.build(verbose=verbose)
+    from . import buildlib
+    return buildlib.build(verbose=verbose)
 
 
 def load() -> ctypes.CDLL:
