@@ -41,9 +41,10 @@ enum SimtTile : int { kSimt128x128 = 0, kSimt64x64 = 1, kSimtTileCount = 2 };
 
 // Split-precision tensor-core variants.
 struct SplitPlan {
-  int pieces;    // bf16 pieces per FP32 operand (2 or 3)
-  int products;  // number of piece products accumulated (3, 6 or 9)
-  int block_n;   // CTA tile width (128 or 256)
+  int pieces;        // bf16 pieces per FP32 operand (2 or 3)
+  int products;      // number of piece products accumulated (3, 6 or 9)
+  int block_n;       // CTA tile width (128 or 256)
+  int chunk_kb = 0;  // k-blocks per main-accumulator chunk (0: library default)
 };
 
 // --- tensor maps -------------------------------------------------------

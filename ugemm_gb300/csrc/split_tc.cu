@@ -4,97 +4,128 @@
 //
 // Each FP32 operand element x is written as a sum of bf16 pieces
 //     x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1)
-// which is exact for three pieces (8+8+8 significand bits cover FP32's 24).
-// C = alpha * sum over piece products (ai, bj) of A_i * B_j + beta * C, with
-// every piece product computed by tcgen05.mma (kind::f16, bf16 x bf16 ->
-// FP32 accumulate in TMEM):
-//     BF16x9: all nine products            (products exact, FP32 accumulate)
-//     BF16x6: drop a1b2, a2b1, a2b2        (each ~2^-24 relative)
-//     BF16x3: two pieces, a0b0+a0b1+a1b0   (~2^-16 relative; for studies)
+// (exact for three pieces: 8+8+8 significand bits cover FP32's 24).  The
+// product A*B is the sum of piece products A_i*B_j, each a tcgen05.mma
+// (kind::f16, bf16 x bf16 -> FP32 in TMEM):
+//     BF16x9: all nine products;  BF16x6: drop a1b2, a2b1, a2b2 (~2^-24 each);
+//     BF16x3: two pieces, a0b0 + a0b1 + a1b0 (~2^-16; for error studies).
 //
-// Pipeline:
-//   1. split kernel (one HBM pass per operand): reads op(A) / op(B) in any
-//      transpose and leading dimension, writes the pieces as K-major bf16
-//      planes [pieces][rows][Kp] (Kp = K rounded up to 32, zero padded);
-//   2. GEMM kernel, one CTA per 128 x BN tile of C, 6 warps:
-//        warp 0  TMA producer: one 3-D TMA per operand per stage brings all
-//                pieces of a 32-deep k slice (64-byte swizzle) into a
-//                3-4 stage ring (mbarrier full/empty pairs);
-//        warp 1  allocates TMEM (BN fp32 columns) and, from one thread,
-//                issues the tcgen05.mma stream; tcgen05.commit frees stages;
-//        warps 2-5  epilogue: tcgen05.ld the 128 x BN accumulator (one TMEM
-//                lane per row), alpha/beta, store C (guarded for ragged M, N).
+// Accuracy.  The tensor core adds each MMA's result into the FP32
+// accumulator with truncation (measured: the error grows linearly in K and
+// is biased toward zero), so one long TMEM accumulation is ~30x less accurate
+// than an FP32 FMA loop at K = 8192.  This kernel therefore keeps
+//   * the main product a0*b0 in its own TMEM accumulator, restarted every
+//     `chunk_kb` k-blocks: the epilogue warps drain each chunk into FP32
+//     registers (round-to-nearest adds), so truncation only ever acts on a
+//     short partial sum;
+//   * all correction products (~2^-8 of the main term) in a second TMEM
+//     accumulator over the whole K, issued before the main product of each
+//     k-block so a chunk drain overlaps the correction MMAs.
+// Result: normwise error below the plain FP32 SIMT kernel's at every K.
+//
+// Pipeline (persistent: one CTA per SM walks a static list of output tiles,
+// which serves one GEMM or a group of independent GEMMs):
+//   1. split kernel: reads op(A)/op(B) in any transpose and leading
+//      dimension, writes the pieces as K-major bf16 planes [pieces][rows][Kp]
+//      (Kp = K rounded up to 32, zero padded);
+//   2. GEMM kernel, 10 warps:
+//        warp 0   TMA producer: one 3-D TMA per operand per stage brings all
+//                 pieces of a 32-deep k slice (64-byte swizzle) into a 3-4
+//                 stage ring (mbarrier full/empty pairs);
+//        warp 1   allocates TMEM (2 x BN columns: main + corrections) and,
+//                 from one thread, issues the tcgen05.mma stream;
+//        warps 2-9  epilogue: chunk drains, then alpha/beta and the store of
+//                 the 128 x BN tile (one TMEM lane per row; two warps per
+//                 lane quarter, each owning half of the columns).
 // All mbarrier waits are bounded (ptx.cuh); on a timeout the kernel records
-// an error, skips its remaining work and still frees its TMEM.
+// an error, abandons its remaining work and still frees its TMEM.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "internal.h"
 #include "ptx.cuh"
+#include "split_tc.cuh"
 
 namespace ugemm {
 namespace {
 
-constexpr int kBM = 128;        // rows of C per CTA (UMMA M)
-constexpr int kKB = 32;         // k depth of one stage (bf16: 64 bytes per row)
-constexpr int kRowBytes = kKB * 2;
-constexpr int kThreads = 192;   // 6 warps
 constexpr int kRaster = 8;
 
-// Piece products in issue order, encoded (ia << 2) | ib.
-__constant__ uint8_t kProducts[9] = {0x0, 0x1, 0x4, 0x2, 0x5, 0x8, 0x6, 0x9, 0xA};
-
-template <int NP, int BN>
-struct TcShape {
-  static constexpr int A_PLANE = kBM * kRowBytes;   // bytes of one A piece tile
-  static constexpr int B_PLANE = BN * kRowBytes;
-  static constexpr int A_BYTES = NP * A_PLANE;
-  static constexpr int B_BYTES = NP * B_PLANE;
-  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-  static constexpr int STAGES = (220 * 1024) / STAGE_BYTES > 4 ? 4 : (220 * 1024) / STAGE_BYTES;
-  static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
-  static_assert(STAGES >= 2, "pipeline needs two stages");
-};
+// Correction products in issue order, encoded (ia << 2) | ib; the main
+// product a0*b0 is implicit.
+__constant__ uint8_t kCorrections[8] = {0x1, 0x4, 0x2, 0x5, 0x8, 0x6, 0x9, 0xA};
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-template <int NP, int BN>
-__global__ void __launch_bounds__(kThreads, 1)
+__device__ __forceinline__ void fence_tensormap(const CUtensorMap* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                   reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
+
+// Index of the problem owning global tile t (tile_start is ascending).
+__device__ __forceinline__ int find_problem(const TcProblem* probs, int n, int t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct TileCoord { int p, m0, n0; };
+
+template <int BN, bool GROUPED>
+__device__ __forceinline__ TileCoord tile_coord(const TcProblem& single, const TcProblem* probs,
+                                                int nprob, int t, TcProblem& P) {
+  TileCoord tc;
+  tc.p = GROUPED ? find_problem(probs, nprob, t) : 0;
+  P = GROUPED ? probs[tc.p] : single;
+  const int local = t - P.tile_start;
+  const int per_group = kRaster * P.tiles_n;
+  const int first_m = (local / per_group) * kRaster;
+  const int group_rows = min(P.tiles_m - first_m, kRaster);
+  tc.m0 = (first_m + (local % per_group) % group_rows) * kTcBM;
+  tc.n0 = ((local % per_group) / group_rows) * BN;
+  return tc;
+}
+
+template <int NP, int BN, bool GROUPED>
+__global__ void __launch_bounds__(kTcThreads, 1)
     split_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                    float* __restrict__ C, int M, int N, int ldc, float alpha, float beta, int nkb,
-                    int nprod, int tiles_m, int tiles_n, int* err) {
+                    const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
+                    const TcProblem* __restrict__ probs, int nprob, int total_tiles, int nprod,
+                    int chunk_kb, int* err) {
   using S = TcShape<NP, BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S::STAGES * S::STAGE_BYTES);
   uint64_t* empty = full + S::STAGES;
-  uint64_t* accum = empty + S::STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
-
-  const int b = blockIdx.x;
-  const int per_group = kRaster * tiles_n;
-  const int first_m = (b / per_group) * kRaster;
-  const int group_rows = min(tiles_m - first_m, kRaster);
-  const int tile_m = first_m + (b % per_group) % group_rows;
-  const int tile_n = (b % per_group) / group_rows;
-  const int m0 = tile_m * kBM, n0 = tile_n * BN;
+  uint64_t* main_full = empty + S::STAGES;   // a main-product chunk is complete
+  uint64_t* main_empty = main_full + 1;      // the epilogue drained it
+  uint64_t* tile_full = main_empty + 1;      // all MMAs of a tile are complete
+  uint64_t* tmem_empty = tile_full + 1;      // the epilogue read both accumulators
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tmem_empty + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
   if (threadIdx.x == 0) {
     for (int s = 0; s < S::STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    mbar_init(main_full, 1);
+    mbar_init(main_empty, kTcEpiWarps);
+    mbar_init(tile_full, 1);
+    mbar_init(tmem_empty, kTcEpiWarps);
     fence_barrier_init();
   }
   if (warp == 1) {
-    tmem_alloc(tmem_slot, BN);
+    tmem_alloc(tmem_slot, S::TMEM_COLS);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -103,93 +134,167 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    // ------------------------------------------------ TMA producer
+    // ------------------------------------------------------ TMA producer
     if (lane == 0) {
-      tma_prefetch_desc(&tmA);
-      tma_prefetch_desc(&tmB);
-      int issued = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % S::STAGES;
-        const uint32_t ph = (kb / S::STAGES) & 1;
-        if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) break;
-        uint8_t* sa = smem + s * S::STAGE_BYTES;
-        mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-        tma_load_3d(sa, &tmA, &full[s], kb * kKB, m0, 0);
-        tma_load_3d(sa + S::A_BYTES, &tmB, &full[s], kb * kKB, n0, 0);
-        issued = kb + 1;
+      if (!GROUPED) {
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
       }
-      // After a fault elsewhere, let in-flight copies land before exit.
-      if (issued < nkb && issued > 0) {
-        for (int kb = max(0, issued - S::STAGES); kb < issued; ++kb)
-          mbar_wait(&full[kb % S::STAGES], (kb / S::STAGES) & 1, nullptr, 0);
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x) {
+        TcProblem P;
+        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+        const CUtensorMap* ma = GROUPED ? &maps[2 * tc.p] : &tmA;
+        const CUtensorMap* mb = GROUPED ? &maps[2 * tc.p + 1] : &tmB;
+        if (GROUPED) {
+          fence_tensormap(ma);
+          fence_tensormap(mb);
+        }
+        for (int kb = 0; kb < P.nkb; ++kb, ++it) {
+          const int s = it % S::STAGES;
+          const uint32_t ph = (it / S::STAGES) & 1;
+          if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
+          uint8_t* sa = smem + s * S::STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
+          tma_load_3d(sa, ma, &full[s], kb * kTcKB, tc.m0, 0);
+          tma_load_3d(sa + S::A_BYTES, mb, &full[s], kb * kTcKB, tc.n0, 0);
+        }
+      }
+      if (!ok) {  // let copies still in flight land before the CTA exits
+        for (uint32_t j = (it > uint32_t(S::STAGES) ? it - S::STAGES : 0); j < it; ++j)
+          mbar_wait(&full[j % S::STAGES], (j / S::STAGES) & 1, nullptr, 0);
       }
     }
   } else if (warp == 1) {
-    // ------------------------------------------------ MMA issuer
+    // ------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = umma_idesc(1, 1, kBM, BN);
-      const uint32_t a_base = smem_u32(smem);
-      uint32_t acc_flag = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % S::STAGES;
-        const uint32_t ph = (kb / S::STAGES) & 1;
-        if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) break;
-        tc_fence_after();
-        const uint32_t sa = a_base + s * S::STAGE_BYTES;
-        const uint32_t sb = sa + S::A_BYTES;
-        for (int p = 0; p < nprod; ++p) {
-          const uint32_t code = kProducts[p];
-          const uint32_t ia = code >> 2, ib = code & 3;
-#pragma unroll
-          for (int kk = 0; kk < kKB / 16; ++kk) {
-            const uint64_t ad = umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, 512, 4);
-            const uint64_t bd = umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, 512, 4);
-            umma_bf16(tmem, ad, bd, idesc, acc_flag);
-            acc_flag = 1;
-          }
+      constexpr uint32_t idesc = umma_idesc(1, 1, kTcBM, BN);
+      const uint32_t base = smem_u32(smem);
+      const uint32_t t_main = tmem, t_corr = tmem + BN;
+      uint32_t it = 0, nbound = 0, ntile = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
+        TcProblem P;
+        tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+        if (ntile > 0 && !mbar_wait(tmem_empty, (ntile - 1) & 1, err, kDevTimeoutAccum)) {
+          ok = false;
+          break;
         }
-        umma_commit(&empty[s]);
+        tc_fence_after();
+        for (int kb = 0; kb < P.nkb; ++kb, ++it) {
+          const int s = it % S::STAGES;
+          const uint32_t ph = (it / S::STAGES) & 1;
+          if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sa = base + s * S::STAGE_BYTES;
+          const uint32_t sb = sa + S::A_BYTES;
+          // correction products into their own accumulator
+          for (int p = 0; p < nprod - 1; ++p) {
+            const uint32_t code = kCorrections[p];
+            const uint32_t ia = code >> 2, ib = code & 3;
+#pragma unroll
+            for (int kk = 0; kk < kTcKB / 16; ++kk)
+              umma_bf16(t_corr, umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, 512, 4),
+                        umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, 512, 4), idesc,
+                        (kb | p | kk) != 0);
+          }
+          // main product; a new chunk restarts the accumulator once drained
+          const bool chunk_start = (kb % chunk_kb) == 0;
+          if (chunk_start && kb > 0) {
+            if (!mbar_wait(main_empty, nbound & 1, err, kDevTimeoutAccum)) { ok = false; break; }
+            ++nbound;
+            tc_fence_after();
+          }
+#pragma unroll
+          for (int kk = 0; kk < kTcKB / 16; ++kk)
+            umma_bf16(t_main, umma_smem_desc(sa + kk * 32, 512, 4),
+                      umma_smem_desc(sb + kk * 32, 512, 4), idesc, !(chunk_start && kk == 0));
+          umma_commit(&empty[s]);
+          if ((kb + 1) % chunk_kb == 0 && kb + 1 < P.nkb) umma_commit(main_full);
+        }
+        umma_commit(tile_full);
       }
-      umma_commit(accum);
     }
     __syncwarp();
   } else {
-    // ------------------------------------------------ epilogue warps 2..5
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
-    const int row = m0 + q * 32 + lane;
-    const bool wait_ok = __all_sync(0xffffffffu, mbar_wait(accum, 0, err, kDevTimeoutAccum));
-    tc_fence_after();
-    if (wait_ok) {  // warp-uniform: tcgen05.ld is .sync.aligned
-      const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
-      float* crow = C + static_cast<size_t>(row) * ldc;
-#pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
-        uint32_t r[32];
-        tmem_ld_32x32b_x32(tmem + (static_cast<uint32_t>(q * 32) << 16) + c * 32, r);
-        tmem_ld_wait();
-        if (row < M) {
-          const int col0 = n0 + c * 32;
-          if (vec && col0 + 32 <= N) {
+    // ------------------------------------------------------ epilogue warps
+    constexpr int HALF = BN / 2;  // columns per epilogue warp
+    const int ew = warp - 2;
+    const int q = warp & 3;       // TMEM lane quarter this warp may access
+    const int col_off = (ew >> 2) * HALF;
+    const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
+    uint32_t nbound = 0, ntile = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
+      TcProblem P;
+      const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+      float acc[HALF];
 #pragma unroll
-            for (int j = 0; j < 32; j += 4) {
-              float4 v = make_float4(alpha * __uint_as_float(r[j]), alpha * __uint_as_float(r[j + 1]),
-                                     alpha * __uint_as_float(r[j + 2]),
-                                     alpha * __uint_as_float(r[j + 3]));
-              if (beta != 0.f) {
-                const float4 o = *reinterpret_cast<const float4*>(crow + col0 + j);
-                v.x += beta * o.x; v.y += beta * o.y; v.z += beta * o.z; v.w += beta * o.w;
-              }
-              *reinterpret_cast<float4*>(crow + col0 + j) = v;
+      for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
+      const int nchunks = (P.nkb + chunk_kb - 1) / chunk_kb;
+      for (int c = 0; c + 1 < nchunks; ++c) {
+        if (!__all_sync(0xffffffffu, mbar_wait(main_full, nbound & 1, err, kDevTimeoutAccum))) {
+          ok = false;
+          break;
+        }
+        ++nbound;
+        tc_fence_after();
+#pragma unroll
+        for (int c32 = 0; c32 < HALF / 32; ++c32) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(tmem + lane_base + col_off + c32 * 32, r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(main_empty);
+      }
+      if (!ok) break;
+      if (!__all_sync(0xffffffffu, mbar_wait(tile_full, ntile & 1, err, kDevTimeoutAccum))) break;
+      tc_fence_after();
+      // last main chunk, then the corrections (one 32-column slice live at a time)
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+#pragma unroll
+        for (int c32 = 0; c32 < HALF / 32; ++c32) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(tmem + lane_base + part * BN + col_off + c32 * 32, r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tmem_empty);
+      // alpha/beta epilogue straight from registers (C not read when beta == 0)
+      const int row = tc.m0 + q * 32 + lane;
+      if (row < P.M) {
+        float* crow = P.C + static_cast<size_t>(row) * P.ldc;
+        const int col0 = tc.n0 + col_off;
+        const bool vec = ((P.ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(P.C) & 15) == 0);
+        if (vec && col0 + HALF <= P.N) {
+#pragma unroll
+          for (int j = 0; j < HALF; j += 4) {
+            float4 v = make_float4(P.alpha * acc[j], P.alpha * acc[j + 1], P.alpha * acc[j + 2],
+                                   P.alpha * acc[j + 3]);
+            if (P.beta != 0.f) {
+              const float4 o = *reinterpret_cast<const float4*>(crow + col0 + j);
+              v.x += P.beta * o.x; v.y += P.beta * o.y; v.z += P.beta * o.z; v.w += P.beta * o.w;
             }
-          } else {
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (col0 + j < N) {
-                float v = alpha * __uint_as_float(r[j]);
-                if (beta != 0.f) v += beta * crow[col0 + j];
-                crow[col0 + j] = v;
-              }
+            *reinterpret_cast<float4*>(crow + col0 + j) = v;
           }
+        } else {
+#pragma unroll
+          for (int j = 0; j < HALF; ++j)
+            if (col0 + j < P.N) {
+              float v = P.alpha * acc[j];
+              if (P.beta != 0.f) v += P.beta * crow[col0 + j];
+              crow[col0 + j] = v;
+            }
         }
       }
     }
@@ -199,20 +304,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, BN);
+    tmem_dealloc(tmem, S::TMEM_COLS);
   }
 }
 
-// Split op(X) (rows x K, element (r, k) at src[r*sr + k*sk]) into NP bf16
-// planes dst[p][rows][Kp], K-major, zero for k >= K.  One block: 32 rows x
-// 64 k through shared memory, so both source layouts read coalesced.
+// ---------------------------------------------------------------- split pass
+// One 32-row x 64-k tile of op(X) (element (r, k) at src[r*sr + k*sk]) into
+// NP bf16 planes dst[p][rows][Kp], through shared memory so that both source
+// layouts are read coalesced.  Zero for k >= K.
 template <int NP>
-__global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restrict__ src,
-                                                           long long sr, long long sk, int rows,
-                                                           int K, int Kp,
-                                                           __nv_bfloat16* __restrict__ dst) {
-  __shared__ float tile[32][65];
-  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
+__device__ __forceinline__ void split_tile(const float* __restrict__ src, long long sr,
+                                           long long sk, int rows, int K, int Kp,
+                                           __nv_bfloat16* __restrict__ dst, int r0, int k0,
+                                           float (*tile)[65]) {
   const int t = threadIdx.x;
   if (sk == 1) {
     const int k = k0 + (t & 63);
@@ -230,37 +334,62 @@ __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restri
     }
   }
   __syncthreads();
-  const int kp = t & 31;  // k pair within the tile
+  const int kp = t & 31;
   const int k = k0 + 2 * kp;
-  if (k >= Kp) return;
-  const size_t plane = static_cast<size_t>(rows) * Kp;
+  if (k < Kp) {
+    const size_t plane = static_cast<size_t>(rows) * Kp;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int rr = (t >> 5) + 8 * i, r = r0 + rr;
-    if (r >= rows) continue;
-    float x[2] = {tile[rr][2 * kp], tile[rr][2 * kp + 1]};
-    __nv_bfloat16 pc[3][2];
+    for (int i = 0; i < 4; ++i) {
+      const int rr = (t >> 5) + 8 * i, r = r0 + rr;
+      if (r >= rows) continue;
+      __nv_bfloat16 pc[3][2];
 #pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      float rem = x[e];
+      for (int e = 0; e < 2; ++e) {
+        float rem = tile[rr][2 * kp + e];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          pc[p][e] = __float2bfloat16_rn(rem);
+          rem = rem - __bfloat162float(pc[p][e]);
+        }
+      }
+      const size_t off = static_cast<size_t>(r) * Kp + k;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        pc[p][e] = __float2bfloat16_rn(rem);
-        rem = rem - __bfloat162float(pc[p][e]);
+        __nv_bfloat162 v;
+        v.x = pc[p][0];
+        v.y = pc[p][1];
+        *reinterpret_cast<__nv_bfloat162*>(dst + p * plane + off) = v;
       }
-    }
-    const size_t off = static_cast<size_t>(r) * Kp + k;
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      __nv_bfloat162 v;
-      v.x = pc[p][0];
-      v.y = pc[p][1];
-      *reinterpret_cast<__nv_bfloat162*>(dst + p * plane + off) = v;
     }
   }
 }
 
-int kp_of(int K) { return static_cast<int>(align_up(std::max(K, 1), kKB)); }
+template <int NP>
+__global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restrict__ src,
+                                                           long long sr, long long sk, int rows,
+                                                           int K, int Kp,
+                                                           __nv_bfloat16* __restrict__ dst) {
+  __shared__ float tile[32][65];
+  split_tile<NP>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile);
+}
+
+// Many operands in one launch: block b works on the job owning tile b.
+template <int NP>
+__global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
+                                                                   int njobs) {
+  __shared__ float tile[32][65];
+  int lo = 0, hi = njobs - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
+  }
+  const SplitJob j = jobs[lo];
+  const int local = b - j.tile_start;
+  const int tiles_k = (j.Kp + 63) / 64;
+  split_tile<NP>(j.src, j.sr, j.sk, j.rows, j.K, j.Kp, j.dst, (local / tiles_k) * 32,
+                 (local % tiles_k) * 64, tile);
+}
 
 template <int NP>
 void launch_split(const float* src, long long sr, long long sk, int rows, int K, int Kp,
@@ -271,19 +400,24 @@ void launch_split(const float* src, long long sr, long long sk, int rows, int K,
   prof_end(st, kProfSplitPrep);
 }
 
-template <int NP, int BN>
-ugemm_status launch_gemm(const Gemm& g, int nprod, const __nv_bfloat16* ap,
-                         const __nv_bfloat16* bp, int Kp, int* dev_err, cudaStream_t st) {
+int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  return sms;
+}
+
+template <int NP, int BN, bool GROUPED>
+ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcProblem& single,
+                           const CUtensorMap* maps, const TcProblem* probs, int nprob,
+                           int total_tiles, int nprod, int chunk_kb, int max_ctas, int* dev_err,
+                           cudaStream_t st) {
   using S = TcShape<NP, BN>;
-  CUtensorMap ta, tb;
-  const uint64_t row = uint64_t(Kp) * 2;
-  if (!encode_tmap_3d(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ap, Kp, g.M, NP, row, row * g.M,
-                      kKB, kBM, NP, CU_TENSOR_MAP_SWIZZLE_64B))
-    return UGEMM_ERR_CUDA;
-  if (!encode_tmap_3d(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bp, Kp, g.N, NP, row, row * g.N,
-                      kKB, BN, NP, CU_TENSOR_MAP_SWIZZLE_64B))
-    return UGEMM_ERR_CUDA;
-  auto kern = split_tc_kernel<NP, BN>;
+  auto kern = split_tc_kernel<NP, BN, GROUPED>;
   static bool attr_set = false;
   if (!attr_set) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -291,15 +425,27 @@ ugemm_status launch_gemm(const Gemm& g, int nprod, const __nv_bfloat16* ap,
       return UGEMM_ERR_CUDA;
     attr_set = true;
   }
-  const int tiles_m = cdiv(g.M, kBM), tiles_n = cdiv(g.N, BN);
+  const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
-  kern<<<tiles_m * tiles_n, kThreads, S::SMEM, st>>>(ta, tb, g.C, g.M, g.N, g.ldc, g.alpha, g.beta,
-                                                      Kp / kKB, nprod, tiles_m, tiles_n, dev_err);
-  prof_end(st, kProfSplitGemm);
+  kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, nprob, total_tiles, nprod,
+                                          chunk_kb, dev_err);
+  prof_end(st, GROUPED ? kProfGrouped : kProfSplitGemm);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
 
+int kp_of(int K) { return static_cast<int>(align_up(std::max(K, 1), kTcKB)); }
+
 }  // namespace
+
+int split_default_chunk_kb() {
+  static int chunk = 0;
+  if (!chunk) {
+    const char* e = std::getenv("UGEMM_CHUNK_K");
+    const int k = e ? std::atoi(e) : 256;
+    chunk = std::max(1, k / kTcKB);
+  }
+  return chunk;
+}
 
 SplitPlan split_plan_for(int precision, const Gemm& g) {
   SplitPlan p;
@@ -312,32 +458,105 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
   return p;
 }
 
+size_t split_operand_bytes(int pieces, int rows, int K) {
+  return align_up(size_t(pieces) * rows * kp_of(K) * 2, 256);
+}
+
 size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p) {
-  const size_t kp = kp_of(g.K);
-  return align_up(size_t(p.pieces) * g.M * kp * 2, 256) + align_up(size_t(p.pieces) * g.N * kp * 2, 256);
+  return split_operand_bytes(p.pieces, g.M, g.K) + split_operand_bytes(p.pieces, g.N, g.K);
+}
+
+bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
+                       int K, CUtensorMap* ta, CUtensorMap* tb) {
+  const int Kp = kp_of(K);
+  const uint64_t row = uint64_t(Kp) * 2;
+  return encode_tmap_3d(ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ap, Kp, M, pieces, row, row * M,
+                        kTcKB, kTcBM, pieces, CU_TENSOR_MAP_SWIZZLE_64B) &&
+         encode_tmap_3d(tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bp, Kp, N, pieces, row, row * N,
+                        kTcKB, block_n, pieces, CU_TENSOR_MAP_SWIZZLE_64B);
+}
+
+TcProblem split_problem(const Gemm& g, int block_n, int tile_start) {
+  TcProblem P;
+  P.C = g.C;
+  P.M = g.M;
+  P.N = g.N;
+  P.ldc = g.ldc;
+  P.alpha = g.alpha;
+  P.beta = g.beta;
+  P.nkb = kp_of(g.K) / kTcKB;
+  P.tiles_m = cdiv(g.M, kTcBM);
+  P.tiles_n = cdiv(g.N, block_n);
+  P.tile_start = tile_start;
+  return P;
+}
+
+// op(A)[m][k]: 'N' -> A[m*lda + k];  'T' -> A[k*lda + m]
+// op(B)^T[n][k]: 'N' -> B[k*ldb + n]; 'T' -> B[n*ldb + k]
+void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
+                           long long* b_sk) {
+  *a_sr = g.ta == 'N' ? g.lda : 1;
+  *a_sk = g.ta == 'N' ? 1 : g.lda;
+  *b_sr = g.tb == 'N' ? 1 : g.ldb;
+  *b_sk = g.tb == 'N' ? g.ldb : 1;
 }
 
 ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* dev_err,
                           cudaStream_t st) {
   const int Kp = kp_of(g.K);
-  const size_t a_bytes = align_up(size_t(p.pieces) * g.M * Kp * 2, 256);
   if (split_scratch_bytes(g, p) > ws.bytes) return UGEMM_ERR_ARENA_TOO_SMALL;
   auto* ap = static_cast<__nv_bfloat16*>(ws.ptr);
-  auto* bp = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(ws.ptr) + a_bytes);
-  // op(A)[m][k]:  'N' -> A[m*lda + k];  'T' -> A[k*lda + m]
-  const long long a_sr = g.ta == 'N' ? g.lda : 1, a_sk = g.ta == 'N' ? 1 : g.lda;
-  // op(B)^T[n][k]: 'N' -> B[k*ldb + n]; 'T' -> B[n*ldb + k]
-  const long long b_sr = g.tb == 'N' ? 1 : g.ldb, b_sk = g.tb == 'N' ? g.ldb : 1;
+  auto* bp = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(ws.ptr) +
+                                               split_operand_bytes(p.pieces, g.M, g.K));
+  long long a_sr, a_sk, b_sr, b_sk;
+  split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
   if (p.pieces == 3) {
     launch_split<3>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
     launch_split<3>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
-    if (p.block_n == 256) return launch_gemm<3, 256>(g, p.products, ap, bp, Kp, dev_err, st);
-    return launch_gemm<3, 128>(g, p.products, ap, bp, Kp, dev_err, st);
+  } else {
+    launch_split<2>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
+    launch_split<2>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
   }
-  launch_split<2>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
-  launch_split<2>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
-  if (p.block_n == 256) return launch_gemm<2, 256>(g, p.products, ap, bp, Kp, dev_err, st);
-  return launch_gemm<2, 128>(g, p.products, ap, bp, Kp, dev_err, st);
+  CUtensorMap ta, tb;
+  if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb))
+    return UGEMM_ERR_CUDA;
+  const TcProblem P = split_problem(g, p.block_n, 0);
+  const int total = P.tiles_m * P.tiles_n;
+  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, 1, total, chunk, 0, dev_err, st);
 }
+
+ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,
+                               const TcProblem& single, const CUtensorMap* maps,
+                               const TcProblem* probs, int nprob, int total_tiles, int chunk_kb,
+                               int max_ctas, int* dev_err, cudaStream_t st) {
+  const bool grouped = probs != nullptr;
+#define UGEMM_SPLIT_CASE(NP, BN)                                                              \
+  if (p.pieces == NP && p.block_n == BN)                                                     \
+    return grouped ? launch_kernel<NP, BN, true>(ta, tb, single, maps, probs, nprob,         \
+                                                 total_tiles, p.products, chunk_kb, max_ctas, \
+                                                 dev_err, st)                                 \
+                   : launch_kernel<NP, BN, false>(ta, tb, single, maps, probs, nprob,        \
+                                                  total_tiles, p.products, chunk_kb,         \
+                                                  max_ctas, dev_err, st);
+  UGEMM_SPLIT_CASE(3, 256)
+  UGEMM_SPLIT_CASE(3, 128)
+  UGEMM_SPLIT_CASE(2, 256)
+  UGEMM_SPLIT_CASE(2, 128)
+#undef UGEMM_SPLIT_CASE
+  return UGEMM_ERR_ARG;
+}
+
+ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
+                                  cudaStream_t st) {
+  if (total_tiles <= 0) return UGEMM_OK;
+  prof_begin(st);
+  if (pieces == 3) split_pieces_batched_kernel<3><<<total_tiles, 256, 0, st>>>(jobs, njobs);
+  else split_pieces_batched_kernel<2><<<total_tiles, 256, 0, st>>>(jobs, njobs);
+  prof_end(st, kProfSplitPrep);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+int split_kp(int K) { return kp_of(K); }
 
 }  // namespace ugemm

@@ -1,0 +1,66 @@
+// split_tc.cuh -- types shared by the split-precision tensor-core kernels
+// (split_tc.cu) and the grouped GEMM planner (grouped.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "internal.h"
+
+namespace ugemm {
+
+constexpr int kTcBM = 128;       // rows of C per CTA tile (UMMA M)
+constexpr int kTcKB = 32;        // k depth of one pipeline stage (64-byte bf16 rows)
+constexpr int kTcEpiWarps = 8;   // two per TMEM lane quarter
+constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
+
+template <int NP, int BN>
+struct TcShape {
+  static constexpr int A_PLANE = kTcBM * kTcKB * 2;  // bytes of one A piece tile
+  static constexpr int B_PLANE = BN * kTcKB * 2;
+  static constexpr int A_BYTES = NP * A_PLANE;
+  static constexpr int B_BYTES = NP * B_PLANE;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int FIT = (224 * 1024) / STAGE_BYTES;
+  static constexpr int STAGES = FIT > 4 ? 4 : FIT;
+  static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
+  static constexpr uint32_t TMEM_COLS = 2 * BN;  // main + correction accumulators
+  static_assert(STAGES >= 2, "pipeline needs two stages");
+  static_assert(SMEM <= 232448, "shared memory budget");
+};
+
+// One GEMM as the persistent kernel sees it (device-resident for groups).
+struct TcProblem {
+  float* C;
+  int M, N, ldc;
+  float alpha, beta;
+  int nkb;              // k-blocks of kTcKB
+  int tiles_m, tiles_n;
+  int tile_start;       // first global tile index of this problem
+};
+
+// One operand to split in the batched pre-pass.
+struct SplitJob {
+  const float* src;
+  long long sr, sk;     // element (r, k) at src[r*sr + k*sk]
+  __nv_bfloat16* dst;   // [pieces][rows][Kp]
+  int rows, K, Kp;
+  int tile_start;       // first 32x64 tile index of this job
+};
+
+int split_kp(int K);
+int split_default_chunk_kb();
+size_t split_operand_bytes(int pieces, int rows, int K);
+void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
+                           long long* b_sk);
+bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
+                       int K, CUtensorMap* ta, CUtensorMap* tb);
+TcProblem split_problem(const Gemm& g, int block_n, int tile_start);
+ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,
+                               const TcProblem& single, const CUtensorMap* maps,
+                               const TcProblem* probs, int nprob, int total_tiles, int chunk_kb,
+                               int max_ctas, int* dev_err, cudaStream_t st);
+ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
+                                  cudaStream_t st);
+
+}  // namespace ugemm
