@@ -129,6 +129,61 @@ UGEMM_API int ugemm_sgemm_backward(char transa, char transb, int M, int N, int K
 /* Device information: SM count and compute capability of the current device. */
 UGEMM_API int ugemm_device_info(int *sm_count, int *cc_major, int *cc_minor);
 
+/* ------------------------------------------------------------------ */
+/* Grouped GEMM (spec batching form; no reference counterpart).  */
+/* Many independent row-major problems, one batched pre-pass launch and */
+/* one persistent GEMM launch; the plan can hold a CUDA graph of both.  */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  char transa, transb; /* 'N' or 'T', as in sgemm_cuda */
+  int M, N, K;
+  float alpha, beta;
+  const float *A; /* device pointers */
+  int lda;
+  const float *B;
+  int ldb;
+  float *C;
+  int ldc;
+} ugemm_problem;
+
+/* Tile configuration of a grouped launch (chosen by ugemm_tune_grouped). */
+typedef struct {
+  int block_n;  /* split form: CTA tile width 128 or 256; SIMT form: square tile 64 or 128 */
+  int chunk_k;  /* split form: k depth between main-accumulator drains (multiple of 32) */
+  int max_ctas; /* persistent CTAs; 0 = one per SM */
+} ugemm_tile_config;
+
+typedef struct ugemm_grouped_plan_s ugemm_grouped_plan;
+
+#define UGEMM_PLAN_GRAPH 1 /* capture the plan's launches once into a CUDA graph */
+
+/* Build a plan (allocates its scratch and device tables; do this outside
+ * stream capture).  `config` NULL: the tuned configuration cached for this
+ * problem set (UGEMM_TUNE_CACHE file), else a default.  Problems keep their
+ * device pointers: a plan replays on the same buffers. */
+UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem *problems, int precision,
+                                        const ugemm_tile_config *config, int flags,
+                                        ugemm_grouped_plan **plan);
+/* Enqueue the plan on `stream` (graph launch when built with UGEMM_PLAN_GRAPH). */
+UGEMM_API int ugemm_grouped_run(ugemm_grouped_plan *plan, void *stream);
+/* Synchronise `stream` and report a kernel wait timeout of this plan. */
+UGEMM_API int ugemm_grouped_check(ugemm_grouped_plan *plan, void *stream);
+UGEMM_API int ugemm_grouped_plan_destroy(ugemm_grouped_plan *plan);
+UGEMM_API double ugemm_grouped_flops(const ugemm_grouped_plan *plan);
+UGEMM_API int ugemm_grouped_config(const ugemm_grouped_plan *plan, ugemm_tile_config *config);
+/* One-shot: plan, run, check, destroy (synchronous). */
+UGEMM_API int ugemm_sgemm_grouped(int count, const ugemm_problem *problems, int precision,
+                                  void *stream);
+
+/* Autotuner: time every candidate tile configuration of this problem set
+ * and form on the current device (CUDA events, after warm-up), return the
+ * fastest and remember it in the tuning cache (JSON lines at
+ * $UGEMM_TUNE_CACHE, default ./ugemm_tune_cache.jsonl).  A cached entry is
+ * returned without timing unless `force` is non-zero.  The problems' C
+ * buffers are overwritten while timing. */
+UGEMM_API int ugemm_tune_grouped(int count, const ugemm_problem *problems, int precision,
+                                 int force, ugemm_tile_config *best, double *best_ms);
+
 /* Per-kernel timing for benchmarks (no reference counterpart; the reference's
  * oclTime at ocl.h:344-352 is never enabled).  While enabled, each library
  * kernel launch is bracketed by CUDA events on its own stream.  collect()

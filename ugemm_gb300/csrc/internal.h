@@ -72,6 +72,11 @@ ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st);  // C = beta*C (or 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
+// Grouped plans: default tile configuration and the autotuner's cache.
+ugemm_tile_config default_grouped_config(int form);
+bool tuned_config(int count, const ugemm_problem* problems, int precision, ugemm_tile_config* cfg);
+int split_default_chunk_kb();
+
 // Per-thread last error, shared by the void compat entry points.
 void set_last_error(ugemm_status s, const std::string& msg);
 

@@ -21,25 +21,10 @@
 
 #include "internal.h"
 #include "ptx.cuh"
+#include "simt.cuh"
 
 namespace ugemm {
 namespace {
-
-constexpr int kBK = 16;            // k depth of one pipeline stage
-constexpr int kStages = 4;         // TMA ring depth
-constexpr int kConsumerWarps = 8;  // 16 x 16 compute threads
-constexpr int kThreads = (kConsumerWarps + 1) * 32;
-constexpr int kRaster = 8;         // rows of tiles per raster group (L2 reuse)
-
-template <int TM, int TN>
-struct SimtShape {
-  static constexpr int BM = 16 * TM;
-  static constexpr int BN = 16 * TN;
-  static constexpr int A_BYTES = BM * kBK * 4;
-  static constexpr int B_BYTES = BN * kBK * 4;
-  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-  static constexpr size_t SMEM = 1024 + size_t(kStages) * STAGE_BYTES + 2 * kStages * 8;
-};
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
@@ -49,74 +34,25 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
 // by TMA with CU_TENSOR_MAP_SWIZZLE_64B (address bits [4,6) ^= bits [7,9)).
 __device__ __forceinline__ int sw64_chunk(int r, int q) { return q ^ ((r >> 1) & 3); }
 
-// AK: op(A) rows are k-contiguous (ta == 'N').  BKM: op(B) columns are
-// k-contiguous (tb == 'T').
+// One BM x BN tile's k loop, consuming the TMA ring from stage counter `it`
+// (which keeps running across the tiles of a persistent CTA).  AK: op(A) rows
+// are k-contiguous (ta == 'N').  BKM: op(B) columns are k-contiguous (tb == 'T').
 template <int TM, int TN, bool AK, bool BKM>
-__global__ void __launch_bounds__(kThreads, 1)
-    simt_sgemm_kernel(const __grid_constant__ CUtensorMap tmA,
-                      const __grid_constant__ CUtensorMap tmB, float* __restrict__ C, int M,
-                      int N, int K, int ldc, float alpha, float beta, int tiles_m, int tiles_n,
-                      int* err) {
+__device__ __forceinline__ bool simt_mainloop(const uint8_t* smem, uint64_t* full, uint64_t* empty,
+                                              int nkt, uint32_t& it, float (&acc)[TM][TN],
+                                              int* err) {
   using S = SimtShape<TM, TN>;
   constexpr int BM = S::BM, BN = S::BN;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = align1024(smem_raw);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::STAGE_BYTES);
-  uint64_t* empty = full + kStages;
-
-  // Grouped raster: kRaster consecutive tile rows share their B columns in L2.
-  const int b = blockIdx.x;
-  const int per_group = kRaster * tiles_n;
-  const int first_m = (b / per_group) * kRaster;
-  const int group_rows = min(tiles_m - first_m, kRaster);
-  const int tile_m = first_m + (b % per_group) % group_rows;
-  const int tile_n = (b % per_group) / group_rows;
-  const int m0 = tile_m * BM, n0 = tile_n * BN;
-  const int nkt = (K + kBK - 1) / kBK;
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kConsumerWarps);
-    }
-    fence_barrier_init();
-  }
-  __syncthreads();
-
-  if (warp == kConsumerWarps) {  // ---------------- TMA producer warp
-    if (lane == 0) {
-      tma_prefetch_desc(&tmA);
-      tma_prefetch_desc(&tmB);
-      for (int kt = 0; kt < nkt; ++kt) {
-        const int s = kt % kStages;
-        const uint32_t ph = (kt / kStages) & 1;
-        if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) break;
-        uint8_t* sa = smem + s * S::STAGE_BYTES;
-        uint8_t* sb = sa + S::A_BYTES;
-        mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-        if (AK) tma_load_2d(sa, &tmA, &full[s], kt * kBK, m0);
-        else    tma_load_2d(sa, &tmA, &full[s], m0, kt * kBK);
-        if (BKM) tma_load_2d(sb, &tmB, &full[s], kt * kBK, n0);
-        else     tma_load_2d(sb, &tmB, &full[s], n0, kt * kBK);
-      }
-    }
-    return;
-  }
-
-  // ---------------------------------------------------- consumer warps
+  const int tid = threadIdx.x, lane = tid & 31;
   const int ty = tid >> 4, tx = tid & 15;
-  float acc[TM][TN];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
-
-  bool ok = true;
-  for (int kt = 0; kt < nkt; ++kt) {
-    const int s = kt % kStages;
-    const uint32_t ph = (kt / kStages) & 1;
-    if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) { ok = false; break; }
+  for (int kt = 0; kt < nkt; ++kt, ++it) {
+    const int s = it % kStages;
+    const uint32_t ph = (it / kStages) & 1;
+    if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) return false;
     const float* As = reinterpret_cast<const float*>(smem + s * S::STAGE_BYTES);
     const float* Bs = reinterpret_cast<const float*>(smem + s * S::STAGE_BYTES + S::A_BYTES);
 #pragma unroll
@@ -168,9 +104,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
-  if (!ok) return;
+  return true;
+}
 
-  // ------------------------------------------------------------ epilogue
+// alpha/beta epilogue of one tile from registers; C is not read when beta == 0.
+template <int TM, int TN, bool AK, bool BKM>
+__device__ __forceinline__ void simt_store(const float (&acc)[TM][TN], float* C, int M, int N,
+                                           int ldc, float alpha, float beta, int m0, int n0) {
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;
   const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
 #pragma unroll
   for (int i = 0; i < TM; ++i) {
@@ -209,6 +151,181 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
       }
+    }
+  }
+}
+
+__device__ __forceinline__ void raster_tile(int local, int tiles_m, int tiles_n, int& tile_m,
+                                            int& tile_n) {
+  const int per_group = kRaster * tiles_n;
+  const int first_m = (local / per_group) * kRaster;
+  const int group_rows = min(tiles_m - first_m, kRaster);
+  tile_m = first_m + (local % per_group) % group_rows;
+  tile_n = (local % per_group) / group_rows;
+}
+
+template <int TM, int TN, bool AK, bool BKM>
+__global__ void __launch_bounds__(kThreads, 1)
+    simt_sgemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                      const __grid_constant__ CUtensorMap tmB, float* __restrict__ C, int M,
+                      int N, int K, int ldc, float alpha, float beta, int tiles_m, int tiles_n,
+                      int* err) {
+  using S = SimtShape<TM, TN>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::STAGE_BYTES);
+  uint64_t* empty = full + kStages;
+  int tile_m, tile_n;
+  raster_tile(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
+  const int m0 = tile_m * S::BM, n0 = tile_n * S::BN;
+  const int nkt = (K + kBK - 1) / kBK;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  if (warp == kConsumerWarps) {  // ---------------- TMA producer warp
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      for (int kt = 0; kt < nkt; ++kt) {
+        const int s = kt % kStages;
+        const uint32_t ph = (kt / kStages) & 1;
+        if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) break;
+        uint8_t* sa = smem + s * S::STAGE_BYTES;
+        uint8_t* sb = sa + S::A_BYTES;
+        mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
+        if (AK) tma_load_2d(sa, &tmA, &full[s], kt * kBK, m0);
+        else    tma_load_2d(sa, &tmA, &full[s], m0, kt * kBK);
+        if (BKM) tma_load_2d(sb, &tmB, &full[s], kt * kBK, n0);
+        else     tma_load_2d(sb, &tmB, &full[s], n0, kt * kBK);
+      }
+    }
+    return;
+  }
+  float acc[TM][TN];
+  uint32_t it = 0;
+  if (!simt_mainloop<TM, TN, AK, BKM>(smem, full, empty, nkt, it, acc, err)) return;
+  simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0);
+}
+
+// Persistent grouped SIMT GEMM: one CTA per SM walks the tiles of all
+// problems.  Operands were packed k-contiguous (A as M x Kpad, B as N x Kpad)
+// by the batched pre-pass, so every problem uses the (AK, BKM) layout.
+template <int TM, int TN>
+__global__ void __launch_bounds__(kThreads, 1)
+    simt_grouped_kernel(const CUtensorMap* __restrict__ maps, const SimtProblem* __restrict__ probs,
+                        int nprob, int total_tiles, int* err) {
+  using S = SimtShape<TM, TN>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::STAGE_BYTES);
+  uint64_t* empty = full + kStages;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+  auto locate = [&](int t, SimtProblem& P, int& p, int& m0, int& n0) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
+    }
+    p = lo;
+    P = probs[lo];
+    int tm, tn;
+    raster_tile(t - P.tile_start, P.tiles_m, P.tiles_n, tm, tn);
+    m0 = tm * S::BM;
+    n0 = tn * S::BN;
+  };
+  if (warp == kConsumerWarps) {
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x) {
+        SimtProblem P;
+        int p, m0, n0;
+        locate(t, P, p, m0, n0);
+        const CUtensorMap* ma = &maps[2 * p];
+        const CUtensorMap* mb = &maps[2 * p + 1];
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                         reinterpret_cast<uint64_t>(ma)) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                         reinterpret_cast<uint64_t>(mb)) : "memory");
+        for (int kt = 0; kt < P.nkt; ++kt, ++it) {
+          const int s = it % kStages;
+          const uint32_t ph = (it / kStages) & 1;
+          if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
+          uint8_t* sa = smem + s * S::STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
+          tma_load_2d(sa, ma, &full[s], kt * kBK, m0);
+          tma_load_2d(sa + S::A_BYTES, mb, &full[s], kt * kBK, n0);
+        }
+      }
+    }
+    return;
+  }
+  uint32_t it = 0;
+  for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+    SimtProblem P;
+    int p, m0, n0;
+    locate(t, P, p, m0, n0);
+    float acc[TM][TN];
+    if (!simt_mainloop<TM, TN, true, true>(smem, full, empty, P.nkt, it, acc, err)) return;
+    simt_store<TM, TN, true, true>(acc, P.C, P.M, P.N, P.ldc, P.alpha, P.beta, m0, n0);
+  }
+}
+
+// Batched pre-pass of the grouped SIMT form: copy op(X) (element (r, k) at
+// src[r*sr + k*sk]) into a k-contiguous FP32 matrix dst[rows][ld], 32 x 64
+// tiles through shared memory so both source layouts read coalesced.
+__global__ void __launch_bounds__(256) pack_kmajor_batched_kernel(const PackJob* __restrict__ jobs,
+                                                                  int njobs) {
+  __shared__ float tile[32][65];
+  int lo = 0, hi = njobs - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
+  }
+  const PackJob j = jobs[lo];
+  const int local = b - j.tile_start;
+  const int tiles_k = (j.K + 63) / 64;
+  const int r0 = (local / tiles_k) * 32, k0 = (local % tiles_k) * 64;
+  const int t = threadIdx.x;
+  if (j.sk == 1) {
+    const int k = k0 + (t & 63);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int rr = (t >> 6) + 4 * i, r = r0 + rr;
+      tile[rr][t & 63] = (r < j.rows && k < j.K) ? j.src[r * j.sr + k] : 0.f;
+    }
+  } else {
+    const int rr = t & 31, r = r0 + rr;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int kk = (t >> 5) + 8 * i, k = k0 + kk;
+      tile[rr][kk] = (r < j.rows && k < j.K) ? j.src[r * j.sr + k * j.sk] : 0.f;
+    }
+  }
+  __syncthreads();
+  const int k = k0 + (t & 63);
+  if (k < j.K) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int rr = (t >> 6) + 4 * i, r = r0 + rr;
+      if (r < j.rows) j.dst[static_cast<size_t>(r) * j.ld + k] = tile[rr][t & 63];
     }
   }
 }
@@ -349,6 +466,57 @@ ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st) {
   scale_kernel<<<std::min<size_t>(4096, (total + 255) / 256), 256, 0, st>>>(g.C, g.M, g.N, g.ldc,
                                                                             g.beta);
   prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+int simt_block(int tile) { return tile == kSimt64x64 ? 64 : 128; }
+
+bool simt_encode_kmajor(int tile, const float* a, int M, const float* b, int N, int K, int ld_a,
+                        int ld_b, CUtensorMap* ta, CUtensorMap* tb) {
+  const int bm = simt_block(tile);
+  return encode_tmap_2d(ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a, std::max(K, 1), M, ld_a * 4ull,
+                        kBK, bm, CU_TENSOR_MAP_SWIZZLE_64B) &&
+         encode_tmap_2d(tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b, std::max(K, 1), N, ld_b * 4ull,
+                        kBK, bm, CU_TENSOR_MAP_SWIZZLE_64B);
+}
+
+namespace {
+template <int TM, int TN>
+ugemm_status grouped_t(const CUtensorMap* maps, const SimtProblem* probs, int nprob, int total,
+                       int max_ctas, int* dev_err, cudaStream_t st) {
+  using S = SimtShape<TM, TN>;
+  auto kern = simt_grouped_kernel<TM, TN>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(S::SMEM)) != cudaSuccess)
+      return UGEMM_ERR_CUDA;
+    attr_set = true;
+  }
+  int sms = 148, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = std::max(1, std::min(total, max_ctas > 0 ? max_ctas : sms));
+  prof_begin(st);
+  kern<<<grid, kThreads, S::SMEM, st>>>(maps, probs, nprob, total, dev_err);
+  prof_end(st, kProfGrouped);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+}  // namespace
+
+ugemm_status simt_grouped_launch(int tile, const CUtensorMap* maps, const SimtProblem* probs,
+                                 int nprob, int total_tiles, int max_ctas, int* dev_err,
+                                 cudaStream_t st) {
+  if (total_tiles <= 0) return UGEMM_OK;
+  if (tile == kSimt64x64) return grouped_t<4, 4>(maps, probs, nprob, total_tiles, max_ctas, dev_err, st);
+  return grouped_t<8, 8>(maps, probs, nprob, total_tiles, max_ctas, dev_err, st);
+}
+
+ugemm_status pack_batched_launch(const PackJob* jobs, int njobs, int total_tiles, cudaStream_t st) {
+  if (total_tiles <= 0) return UGEMM_OK;
+  prof_begin(st);
+  pack_kmajor_batched_kernel<<<total_tiles, 256, 0, st>>>(jobs, njobs);
+  prof_end(st, kProfSplitPrep);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
 
