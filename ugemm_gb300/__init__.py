@@ -50,6 +50,9 @@ EXPORTS = (
     "ugemm_status_string", "ugemm_sgemm", "ugemm_sgemm_host", "ugemm_sgemm_dev",
     "ugemm_workspace_bytes", "ugemm_reserve_workspace", "ugemm_sgemm_backward",
     "ugemm_device_info", "ugemm_profile_enable", "ugemm_profile_collect",
+    "ugemm_grouped_plan_create", "ugemm_grouped_run", "ugemm_grouped_check",
+    "ugemm_grouped_plan_destroy", "ugemm_grouped_flops", "ugemm_grouped_config",
+    "ugemm_sgemm_grouped", "ugemm_tune_grouped",
 )
 PROF_KINDS = ("simt", "split_prepass", "split_gemm", "aux", "grouped")
 
@@ -250,3 +253,124 @@ def profile_collect() -> dict:
     cnt = (_i * n)()
     _check(load().ugemm_profile_collect(ms, cnt, n))
     return {k: (ms[i], cnt[i]) for i, k in enumerate(PROF_KINDS)}
+
+
+# --------------------------------------------------------------------------
+# Grouped GEMM and autotuner
+# --------------------------------------------------------------------------
+PLAN_GRAPH = 1
+
+
+class Problem(ctypes.Structure):
+    """ugemm_problem: one row-major GEMM of a group (device pointers)."""
+    _fields_ = [("transa", _c), ("transb", _c), ("M", _i), ("N", _i), ("K", _i),
+                ("alpha", _f), ("beta", _f), ("A", _p), ("lda", _i), ("B", _p), ("ldb", _i),
+                ("C", _p), ("ldc", _i)]
+
+
+class TileConfig(ctypes.Structure):
+    """ugemm_tile_config."""
+    _fields_ = [("block_n", _i), ("chunk_k", _i), ("max_ctas", _i)]
+
+    def as_dict(self):
+        return {"block_n": self.block_n, "chunk_k": self.chunk_k, "max_ctas": self.max_ctas}
+
+
+def _grouped_sigs(lib):
+    if getattr(lib, "_grouped_ready", False):
+        return
+    pp = ctypes.POINTER(_p)
+    lib.ugemm_grouped_plan_create.argtypes = [_i, ctypes.POINTER(Problem), _i,
+                                              ctypes.POINTER(TileConfig), _i, pp]
+    lib.ugemm_grouped_plan_create.restype = _i
+    for name in ("ugemm_grouped_run", "ugemm_grouped_check"):
+        getattr(lib, name).argtypes = [_p, _p]
+        getattr(lib, name).restype = _i
+    lib.ugemm_grouped_plan_destroy.argtypes = [_p]
+    lib.ugemm_grouped_plan_destroy.restype = _i
+    lib.ugemm_grouped_flops.argtypes = [_p]
+    lib.ugemm_grouped_flops.restype = ctypes.c_double
+    lib.ugemm_grouped_config.argtypes = [_p, ctypes.POINTER(TileConfig)]
+    lib.ugemm_grouped_config.restype = _i
+    lib.ugemm_sgemm_grouped.argtypes = [_i, ctypes.POINTER(Problem), _i, _p]
+    lib.ugemm_sgemm_grouped.restype = _i
+    lib.ugemm_tune_grouped.argtypes = [_i, ctypes.POINTER(Problem), _i, _i,
+                                       ctypes.POINTER(TileConfig), ctypes.POINTER(ctypes.c_double)]
+    lib.ugemm_tune_grouped.restype = _i
+    lib._grouped_ready = True
+
+
+def make_problems(specs):
+    """specs: iterable of dicts with ta, tb, M, N, K, alpha, beta, A, lda, B, ldb, C, ldc
+    (A/B/C torch CUDA tensors or device addresses)."""
+    specs = list(specs)
+    arr = (Problem * len(specs))()
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    for i, s in enumerate(specs):
+        arr[i] = Problem(s["ta"].encode(), s["tb"].encode(), s["M"], s["N"], s["K"], s["alpha"],
+                         s["beta"], ptr(s["A"]), s["lda"], ptr(s["B"]), s["ldb"], ptr(s["C"]),
+                         s["ldc"])
+    return arr
+
+
+class GroupedPlan:
+    """A grouped GEMM plan (ugemm_grouped_plan); run() is stream-ordered."""
+
+    def __init__(self, problems, precision="bf16x6", config=None, graph=False):
+        lib = load()
+        _grouped_sigs(lib)
+        self._lib = lib
+        self.problems = problems if isinstance(problems, ctypes.Array) else make_problems(problems)
+        cfg = None
+        if config is not None:
+            cfg = ctypes.byref(config if isinstance(config, TileConfig) else TileConfig(**config))
+        h = _p()
+        _check(lib.ugemm_grouped_plan_create(len(self.problems), self.problems, _prec(precision),
+                                             cfg, PLAN_GRAPH if graph else 0, ctypes.byref(h)))
+        self.handle = h
+
+    def run(self, stream=None):
+        _check(self._lib.ugemm_grouped_run(self.handle, _stream_ptr(stream)))
+
+    def check(self, stream=None):
+        _check(self._lib.ugemm_grouped_check(self.handle, _stream_ptr(stream)))
+
+    @property
+    def flops(self) -> float:
+        return float(self._lib.ugemm_grouped_flops(self.handle))
+
+    @property
+    def config(self) -> dict:
+        c = TileConfig()
+        _check(self._lib.ugemm_grouped_config(self.handle, ctypes.byref(c)))
+        return c.as_dict()
+
+    def close(self):
+        if self.handle:
+            self._lib.ugemm_grouped_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tune_grouped(problems, precision="bf16x6", force=False):
+    """Autotune the tile configuration of a problem set; returns (config dict, ms)."""
+    lib = load()
+    _grouped_sigs(lib)
+    arr = problems if isinstance(problems, ctypes.Array) else make_problems(problems)
+    best = TileConfig()
+    ms = ctypes.c_double()
+    _check(lib.ugemm_tune_grouped(len(arr), arr, _prec(precision), 1 if force else 0,
+                                  ctypes.byref(best), ctypes.byref(ms)))
+    return best.as_dict(), ms.value
+
+
+def sgemm_grouped(problems, precision="bf16x6", stream=None):
+    lib = load()
+    _grouped_sigs(lib)
+    arr = problems if isinstance(problems, ctypes.Array) else make_problems(problems)
+    _check(lib.ugemm_sgemm_grouped(len(arr), arr, _prec(precision), _stream_ptr(stream)))
