@@ -184,6 +184,58 @@ UGEMM_API int ugemm_sgemm_grouped(int count, const ugemm_problem *problems, int 
 UGEMM_API int ugemm_tune_grouped(int count, const ugemm_problem *problems, int precision,
                                  int force, ugemm_tile_config *best, double *best_ms);
 
+/* ------------------------------------------------------------------ */
+/* im2col convolution (sgemm_ocl1.h:81-119 im2col, :271-300              */
+/* ocl_convolution).  Activations are C x (B*H*W) ("CNHW"); with B = 1    */
+/* this is the reference's CHW image and its im2col matrix               */
+/* (C*k*k) x (Ho*Wo), row (c*k*k + ki*k + kj), column (i*Wo + j).        */
+/* ------------------------------------------------------------------ */
+UGEMM_API int ugemm_im2col(const float *x, int channels, int batch, int height, int width,
+                           int ksize, int pad, int stride, float *col, void *stream);
+/* Adjoint of ugemm_im2col: x = sum of the col entries that read it (overwrites x). */
+UGEMM_API int ugemm_col2im(const float *col, int channels, int batch, int height, int width,
+                           int ksize, int pad, int stride, float *x, void *stream);
+
+/* A stack of convolutions run as GEMMs: layer l computes
+ *   forward  Y_l = W_l * im2col(X_l)                 (M = cout, N = B*Ho*Wo, K = cin*k*k)
+ *   backward dW_l = dY_l * col_l^T, dcol_l = W_l^T * dY_l (one grouped launch),
+ *            dX_l = col2im(dcol_l) = dY_{l-1}
+ * with X_{l+1} = Y_l.  The gradient entering the last layer is its own
+ * output (loss 0.5 * ||Y_last||^2).  No reference counterpart beyond the
+ * single-layer forward ocl_convolution. */
+typedef struct {
+  int cin, cout, height, width; /* input channels/size of the layer */
+  int ksize, pad, stride;       /* square kernel, equal padding and stride */
+} ugemm_conv_layer;
+
+typedef struct ugemm_conv_stack_s ugemm_conv_stack;
+
+#define UGEMM_CONV_FORWARD 1
+#define UGEMM_CONV_BACKWARD 2
+enum {
+  UGEMM_CONV_X = 0, /* layer input (fill layer 0's before a forward run) */
+  UGEMM_CONV_W = 1, /* weights, cout x cin*k*k (fill before running) */
+  UGEMM_CONV_Y = 2,
+  UGEMM_CONV_COL = 3,
+  UGEMM_CONV_DW = 4,
+  UGEMM_CONV_DCOL = 5,
+  UGEMM_CONV_DX = 6,
+  UGEMM_CONV_DY = 7
+};
+
+/* Allocates every buffer and one grouped plan per layer and direction; with
+ * UGEMM_PLAN_GRAPH the forward, backward and combined sequences are
+ * captured into CUDA graphs. */
+UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer *layers, int batch,
+                                      int precision, int flags, ugemm_conv_stack **stack);
+/* Device pointer and element count of one buffer of one layer. */
+UGEMM_API int ugemm_conv_stack_buffer(ugemm_conv_stack *stack, int layer, int which, float **ptr,
+                                      size_t *count);
+/* Run forward (1), backward (2) or both (3) on `stream`. */
+UGEMM_API int ugemm_conv_stack_run(ugemm_conv_stack *stack, int what, void *stream);
+UGEMM_API double ugemm_conv_stack_flops(const ugemm_conv_stack *stack, int what);
+UGEMM_API int ugemm_conv_stack_destroy(ugemm_conv_stack *stack);
+
 /* Per-kernel timing for benchmarks (no reference counterpart; the reference's
  * oclTime at ocl.h:344-352 is never enabled).  While enabled, each library
  * kernel launch is bracketed by CUDA events on its own stream.  collect()

@@ -374,3 +374,121 @@ def sgemm_grouped(problems, precision="bf16x6", stream=None):
     _grouped_sigs(lib)
     arr = problems if isinstance(problems, ctypes.Array) else make_problems(problems)
     _check(lib.ugemm_sgemm_grouped(len(arr), arr, _prec(precision), _stream_ptr(stream)))
+
+
+# --------------------------------------------------------------------------
+# im2col convolution stack
+# --------------------------------------------------------------------------
+CONV_FORWARD, CONV_BACKWARD = 1, 2
+CONV_BUFFERS = {"x": 0, "w": 1, "y": 2, "col": 3, "dw": 4, "dcol": 5, "dx": 6, "dy": 7}
+
+
+class ConvLayer(ctypes.Structure):
+    """ugemm_conv_layer."""
+    _fields_ = [("cin", _i), ("cout", _i), ("height", _i), ("width", _i), ("ksize", _i),
+                ("pad", _i), ("stride", _i)]
+
+
+def _conv_sigs(lib):
+    if getattr(lib, "_conv_ready", False):
+        return
+    lib.ugemm_im2col.argtypes = [_p, _i, _i, _i, _i, _i, _i, _i, _p, _p]
+    lib.ugemm_im2col.restype = _i
+    lib.ugemm_col2im.argtypes = [_p, _i, _i, _i, _i, _i, _i, _i, _p, _p]
+    lib.ugemm_col2im.restype = _i
+    lib.ugemm_conv_stack_create.argtypes = [_i, ctypes.POINTER(ConvLayer), _i, _i, _i,
+                                            ctypes.POINTER(_p)]
+    lib.ugemm_conv_stack_create.restype = _i
+    lib.ugemm_conv_stack_buffer.argtypes = [_p, _i, _i, ctypes.POINTER(_p), ctypes.POINTER(_sz)]
+    lib.ugemm_conv_stack_buffer.restype = _i
+    lib.ugemm_conv_stack_run.argtypes = [_p, _i, _p]
+    lib.ugemm_conv_stack_run.restype = _i
+    lib.ugemm_conv_stack_flops.argtypes = [_p, _i]
+    lib.ugemm_conv_stack_flops.restype = ctypes.c_double
+    lib.ugemm_conv_stack_destroy.argtypes = [_p]
+    lib.ugemm_conv_stack_destroy.restype = _i
+    lib._conv_ready = True
+
+
+def im2col(x, channels, batch, height, width, ksize, pad, stride, col, stream=None):
+    lib = load()
+    _conv_sigs(lib)
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_im2col(ptr(x), channels, batch, height, width, ksize, pad, stride, ptr(col),
+                            _stream_ptr(stream)))
+
+
+def col2im(col, channels, batch, height, width, ksize, pad, stride, x, stream=None):
+    lib = load()
+    _conv_sigs(lib)
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_col2im(ptr(col), channels, batch, height, width, ksize, pad, stride, ptr(x),
+                            _stream_ptr(stream)))
+
+
+class ConvStack:
+    """ugemm_conv_stack: layers as (cin, cout, height, width, stride[, ksize, pad])."""
+
+    def __init__(self, layers, batch, precision="bf16x6", graph=True):
+        lib = load()
+        _conv_sigs(lib)
+        self._lib = lib
+        arr = (ConvLayer * len(layers))()
+        for i, l in enumerate(layers):
+            cin, cout, h, w, stride = l[:5]
+            k = l[5] if len(l) > 5 else 3
+            pad = l[6] if len(l) > 6 else 1
+            arr[i] = ConvLayer(cin, cout, h, w, k, pad, stride)
+        self.layers = arr
+        self.batch = batch
+        h = _p()
+        _check(lib.ugemm_conv_stack_create(len(arr), arr, batch, _prec(precision),
+                                           PLAN_GRAPH if graph else 0, ctypes.byref(h)))
+        self.handle = h
+
+    def buffer(self, layer: int, which: str):
+        """(device address, element count) of a buffer."""
+        p, n = _p(), _sz()
+        _check(self._lib.ugemm_conv_stack_buffer(self.handle, layer, CONV_BUFFERS[which],
+                                                 ctypes.byref(p), ctypes.byref(n)))
+        return p.value, n.value
+
+    def tensor(self, layer: int, which: str, shape):
+        """A torch view of a stack buffer (no copy)."""
+        import torch
+        addr, n = self.buffer(layer, which)
+        numel = 1
+        for s in shape:
+            numel *= s
+        assert numel == n, (which, shape, n)
+        return _torch_view(addr, shape, torch)
+
+    def run(self, what: int = CONV_FORWARD | CONV_BACKWARD, stream=None):
+        _check(self._lib.ugemm_conv_stack_run(self.handle, what, _stream_ptr(stream)))
+
+    def flops(self, what: int = CONV_FORWARD | CONV_BACKWARD) -> float:
+        return float(self._lib.ugemm_conv_stack_flops(self.handle, what))
+
+    def close(self):
+        if self.handle:
+            self._lib.ugemm_conv_stack_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _torch_view(addr: int, shape, torch):
+    """Wrap library-owned float32 device memory as a torch tensor (no copy)."""
+    class _Holder:
+        pass
+    numel = 1
+    for s in shape:
+        numel *= s
+    h = _Holder()
+    h.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (addr, False),
+                                  "version": 3, "strides": None}
+    return torch.as_tensor(h, device="cuda")

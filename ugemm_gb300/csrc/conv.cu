@@ -1,0 +1,341 @@
+// conv.cu -- im2col / col2im kernels and the im2col convolution stack
+// (forward, dX and dW of every layer as split-precision or SIMT grouped
+// GEMMs, optionally captured in one CUDA graph).
+//
+// The reference convolves one image at a time: its OpenCL im2col
+// (sgemm_ocl1.h:81-119) turns a CHW image into a (C*k*k) x (Ho*Wo) matrix and
+// ocl_convolution (sgemm_ocl1.h:271-300) multiplies the weights
+// (Cout x C*k*k) by it.  Here activations are stored C x (B*H*W) ("CNHW"),
+// so a whole batch is one im2col matrix (C*k*k) x (B*Ho*Wo) and one GEMM per
+// layer; with B = 1 the layout and the im2col result are the reference's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "internal.h"
+
+namespace ugemm {
+namespace {
+
+// col[(c*k*k + ki*k + kj)][(b*Ho + i)*Wo + j] = x[c][b][i*s - p + ki][j*s - p + kj]
+// (0 outside the image).  One thread per (c, b, i, j), as the reference's
+// work-item per (c, i, j) (sgemm_ocl1.h:97-118).
+__global__ void im2col_kernel(const float* __restrict__ x, int C, int B, int H, int W, int k,
+                              int pad, int stride, int Ho, int Wo, float* __restrict__ col) {
+  const long long n_pix = static_cast<long long>(B) * Ho * Wo;
+  const long long total = n_pix * C;
+  for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < total;
+       idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long pix = idx % n_pix;
+    const int c = static_cast<int>(idx / n_pix);
+    const int j = static_cast<int>(pix % Wo);
+    const int i = static_cast<int>((pix / Wo) % Ho);
+    const int b = static_cast<int>(pix / (static_cast<long long>(Wo) * Ho));
+    const int y0 = i * stride - pad, x0 = j * stride - pad;
+    const float* src = x + (static_cast<long long>(c) * B + b) * H * W;
+    float* dst = col + static_cast<long long>(c) * k * k * n_pix + pix;
+    for (int ki = 0; ki < k; ++ki)
+      for (int kj = 0; kj < k; ++kj) {
+        const int yy = y0 + ki, xx = x0 + kj;
+        *dst = (yy >= 0 && xx >= 0 && yy < H && xx < W) ? src[yy * W + xx] : 0.f;
+        dst += n_pix;
+      }
+  }
+}
+
+// Adjoint of im2col: dx[c][b][y][x] = sum of the col entries that read it
+// (gather form: no atomics, deterministic).
+__global__ void col2im_kernel(const float* __restrict__ col, int C, int B, int H, int W, int k,
+                              int pad, int stride, int Ho, int Wo, float* __restrict__ dx) {
+  const long long n_pix = static_cast<long long>(B) * Ho * Wo;
+  const long long total = static_cast<long long>(C) * B * H * W;
+  for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < total;
+       idx += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int xx = static_cast<int>(idx % W);
+    const int yy = static_cast<int>((idx / W) % H);
+    const int b = static_cast<int>((idx / (static_cast<long long>(W) * H)) % B);
+    const int c = static_cast<int>(idx / (static_cast<long long>(W) * H * B));
+    float acc = 0.f;
+    for (int ki = 0; ki < k; ++ki) {
+      const int ty = yy + pad - ki;
+      if (ty < 0 || ty % stride) continue;
+      const int i = ty / stride;
+      if (i >= Ho) continue;
+      for (int kj = 0; kj < k; ++kj) {
+        const int tx = xx + pad - kj;
+        if (tx < 0 || tx % stride) continue;
+        const int j = tx / stride;
+        if (j >= Wo) continue;
+        acc += col[(static_cast<long long>(c) * k * k + ki * k + kj) * n_pix +
+                   (static_cast<long long>(b) * Ho + i) * Wo + j];
+      }
+    }
+    dx[idx] = acc;
+  }
+}
+
+int out_dim(int in, int k, int pad, int stride) { return (in + 2 * pad - k) / stride + 1; }
+
+int grid_for(long long n) {
+  return static_cast<int>(std::min<long long>((n + 255) / 256, 148LL * 32));
+}
+
+}  // namespace
+
+ugemm_status im2col_launch(const float* x, int C, int B, int H, int W, int k, int pad, int stride,
+                           float* col, cudaStream_t st) {
+  const int Ho = out_dim(H, k, pad, stride), Wo = out_dim(W, k, pad, stride);
+  if (Ho <= 0 || Wo <= 0) return UGEMM_ERR_ARG;
+  prof_begin(st);
+  im2col_kernel<<<grid_for(static_cast<long long>(C) * B * Ho * Wo), 256, 0, st>>>(
+      x, C, B, H, W, k, pad, stride, Ho, Wo, col);
+  prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+ugemm_status col2im_launch(const float* col, int C, int B, int H, int W, int k, int pad,
+                           int stride, float* dx, cudaStream_t st) {
+  const int Ho = out_dim(H, k, pad, stride), Wo = out_dim(W, k, pad, stride);
+  if (Ho <= 0 || Wo <= 0) return UGEMM_ERR_ARG;
+  prof_begin(st);
+  col2im_kernel<<<grid_for(static_cast<long long>(C) * B * H * W), 256, 0, st>>>(
+      col, C, B, H, W, k, pad, stride, Ho, Wo, dx);
+  prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+}  // namespace ugemm
+
+// ---------------------------------------------------------------- the stack
+struct ugemm_conv_stack_s {
+  struct Layer {
+    ugemm_conv_layer d;
+    int Ho, Wo;
+    long long n;          // batch * Ho * Wo (GEMM N)
+    int kdim;             // cin * k * k (GEMM K)
+    float *x, *col, *w, *y, *dw, *dcol, *dx;  // dy of layer l is dx of layer l+1
+    ugemm_grouped_plan* fwd = nullptr;
+    ugemm_grouped_plan* bwd = nullptr;
+  };
+  std::vector<Layer> layers;
+  int batch = 0, form = UGEMM_PREC_BF16X6;
+  float* dy_last = nullptr;
+  void* arena = nullptr;
+  double flops_fwd = 0, flops_bwd = 0;
+  cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaGraph_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+using Stack = ugemm_conv_stack_s;
+
+int run_stack(Stack* s, int what, cudaStream_t st) {
+  using namespace ugemm;
+  if (what & UGEMM_CONV_FORWARD) {
+    for (auto& L : s->layers) {
+      ugemm_status r = im2col_launch(L.x, L.d.cin, s->batch, L.d.height, L.d.width, L.d.ksize,
+                                     L.d.pad, L.d.stride, L.col, st);
+      if (r != UGEMM_OK) return r;
+      int rc = ugemm_grouped_run(L.fwd, st);
+      if (rc != UGEMM_OK) return rc;
+    }
+  }
+  if (what & UGEMM_CONV_BACKWARD) {
+    for (int l = static_cast<int>(s->layers.size()) - 1; l >= 0; --l) {
+      auto& L = s->layers[l];
+      int rc = ugemm_grouped_run(L.bwd, st);
+      if (rc != UGEMM_OK) return rc;
+      ugemm_status r = col2im_launch(L.dcol, L.d.cin, s->batch, L.d.height, L.d.width,
+                                     L.d.ksize, L.d.pad, L.d.stride, L.dx, st);
+      if (r != UGEMM_OK) return r;
+    }
+  }
+  return UGEMM_OK;
+}
+
+void destroy_stack(Stack* s) {
+  if (!s) return;
+  for (int i = 0; i < 4; ++i) {
+    if (s->exec[i]) cudaGraphExecDestroy(s->exec[i]);
+    if (s->graph[i]) cudaGraphDestroy(s->graph[i]);
+  }
+  for (auto& L : s->layers) {
+    if (L.fwd) ugemm_grouped_plan_destroy(L.fwd);
+    if (L.bwd) ugemm_grouped_plan_destroy(L.bwd);
+  }
+  if (s->arena) cudaFree(s->arena);
+  delete s;
+}
+}  // namespace
+
+using namespace ugemm;
+
+extern "C" {
+
+UGEMM_API int ugemm_im2col(const float* x, int channels, int batch, int height, int width,
+                           int ksize, int pad, int stride, float* col, void* stream) {
+  if (!x || !col || channels <= 0 || batch <= 0 || height <= 0 || width <= 0 || ksize <= 0 ||
+      pad < 0 || stride <= 0)
+    return UGEMM_ERR_ARG;
+  return im2col_launch(x, channels, batch, height, width, ksize, pad, stride, col,
+                       static_cast<cudaStream_t>(stream));
+}
+
+UGEMM_API int ugemm_col2im(const float* col, int channels, int batch, int height, int width,
+                           int ksize, int pad, int stride, float* x, void* stream) {
+  if (!x || !col || channels <= 0 || batch <= 0 || height <= 0 || width <= 0 || ksize <= 0 ||
+      pad < 0 || stride <= 0)
+    return UGEMM_ERR_ARG;
+  return col2im_launch(col, channels, batch, height, width, ksize, pad, stride, x,
+                       static_cast<cudaStream_t>(stream));
+}
+
+UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layers, int batch,
+                                      int precision, int flags, ugemm_conv_stack** out) {
+  if (!out || nlayers <= 0 || !layers || batch <= 0) return UGEMM_ERR_ARG;
+  *out = nullptr;
+  auto* s = new Stack;
+  s->batch = batch;
+  s->form = precision == UGEMM_PREC_AUTO ? UGEMM_PREC_BF16X6 : precision;
+  // shapes and arena layout
+  size_t bytes = 0;
+  auto take = [&](size_t n) { size_t o = bytes; bytes += align_up(n * sizeof(float), 256); return o; };
+  std::vector<size_t> off;
+  for (int l = 0; l < nlayers; ++l) {
+    const ugemm_conv_layer& d = layers[l];
+    if (d.cin <= 0 || d.cout <= 0 || d.height <= 0 || d.width <= 0 || d.ksize <= 0 || d.pad < 0 ||
+        d.stride <= 0) {
+      destroy_stack(s);
+      return UGEMM_ERR_ARG;
+    }
+    Stack::Layer L{};
+    L.d = d;
+    L.Ho = out_dim(d.height, d.ksize, d.pad, d.stride);
+    L.Wo = out_dim(d.width, d.ksize, d.pad, d.stride);
+    if (L.Ho <= 0 || L.Wo <= 0) { destroy_stack(s); return UGEMM_ERR_ARG; }
+    if (l > 0) {
+      const auto& P = s->layers.back();
+      if (P.d.cout != d.cin || P.Ho != d.height || P.Wo != d.width) {
+        destroy_stack(s);
+        return UGEMM_ERR_ARG;  // layer l must consume layer l-1's output
+      }
+    }
+    L.n = static_cast<long long>(batch) * L.Ho * L.Wo;
+    L.kdim = d.cin * d.ksize * d.ksize;
+    if (L.n > 0x7fffffffLL) { destroy_stack(s); return UGEMM_ERR_ARG; }
+    s->layers.push_back(L);
+  }
+  // arena: x0 | per layer {col, w, y, dw, dcol, dx} | dy_last
+  const size_t x0 = take(size_t(layers[0].cin) * batch * layers[0].height * layers[0].width);
+  for (auto& L : s->layers) {
+    off.push_back(take(size_t(L.kdim) * L.n));                 // col
+    off.push_back(take(size_t(L.d.cout) * L.kdim));            // w
+    off.push_back(take(size_t(L.d.cout) * L.n));               // y
+    off.push_back(take(size_t(L.d.cout) * L.kdim));            // dw
+    off.push_back(take(size_t(L.kdim) * L.n));                 // dcol
+    off.push_back(take(size_t(L.d.cin) * batch * L.d.height * L.d.width));  // dx
+  }
+  if (cudaMalloc(&s->arena, bytes) != cudaSuccess) { s->arena = nullptr; destroy_stack(s); return UGEMM_ERR_ALLOC; }
+  cudaMemset(s->arena, 0, bytes);
+  uint8_t* base = static_cast<uint8_t*>(s->arena);
+  auto at = [&](size_t o) { return reinterpret_cast<float*>(base + o); };
+  for (size_t l = 0; l < s->layers.size(); ++l) {
+    auto& L = s->layers[l];
+    L.x = l == 0 ? at(x0) : s->layers[l - 1].y;
+    L.col = at(off[6 * l]);
+    L.w = at(off[6 * l + 1]);
+    L.y = at(off[6 * l + 2]);
+    L.dw = at(off[6 * l + 3]);
+    L.dcol = at(off[6 * l + 4]);
+    L.dx = at(off[6 * l + 5]);
+  }
+  for (size_t l = 0; l < s->layers.size(); ++l) {
+    auto& L = s->layers[l];
+    const float* dy = (l + 1 < s->layers.size()) ? s->layers[l + 1].dx : nullptr;
+    if (!dy) {
+      s->dy_last = L.y;  // the last layer's output buffer doubles as its incoming gradient slot
+      dy = nullptr;
+    }
+    const int M = L.d.cout, N = static_cast<int>(L.n), K = L.kdim;
+    // forward: y = w * col
+    ugemm_problem f{'N', 'N', M, N, K, 1.f, 0.f, L.w, K, L.col, N, L.y, N};
+    // backward: dw = dy * col^T, dcol = w^T * dy
+    const float* g = dy ? dy : L.y;
+    ugemm_problem b[2] = {{'N', 'T', M, K, N, 1.f, 0.f, g, N, L.col, N, L.dw, K},
+                          {'T', 'N', K, N, M, 1.f, 0.f, L.w, K, g, N, L.dcol, N}};
+    int rc = ugemm_grouped_plan_create(1, &f, s->form, nullptr, 0, &L.fwd);
+    if (rc == UGEMM_OK) rc = ugemm_grouped_plan_create(2, b, s->form, nullptr, 0, &L.bwd);
+    if (rc != UGEMM_OK) { destroy_stack(s); return rc; }
+    s->flops_fwd += 2.0 * M * double(N) * K;
+    s->flops_bwd += 4.0 * M * double(N) * K;
+  }
+  if (flags & UGEMM_PLAN_GRAPH) {
+    for (int what = 1; what <= 3; ++what) {
+      cudaStream_t cs;
+      if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        destroy_stack(s);
+        return UGEMM_ERR_CUDA;
+      }
+      cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      int rc = UGEMM_OK;
+      if (e == cudaSuccess) {
+        rc = run_stack(s, what, cs);
+        e = cudaStreamEndCapture(cs, &s->graph[what]);
+      }
+      if (e == cudaSuccess && rc == UGEMM_OK) e = cudaGraphInstantiate(&s->exec[what], s->graph[what], 0);
+      cudaStreamDestroy(cs);
+      if (e != cudaSuccess || rc != UGEMM_OK) { destroy_stack(s); return UGEMM_ERR_CUDA; }
+    }
+  }
+  *out = s;
+  return UGEMM_OK;
+}
+
+UGEMM_API int ugemm_conv_stack_buffer(ugemm_conv_stack* s, int layer, int which, float** ptr,
+                                      size_t* count) {
+  if (!s || !ptr || layer < 0 || layer >= static_cast<int>(s->layers.size())) return UGEMM_ERR_ARG;
+  const auto& L = s->layers[layer];
+  const size_t x_n = size_t(L.d.cin) * s->batch * L.d.height * L.d.width;
+  size_t n = 0;
+  switch (which) {
+    case UGEMM_CONV_X: *ptr = L.x; n = x_n; break;
+    case UGEMM_CONV_W: *ptr = L.w; n = size_t(L.d.cout) * L.kdim; break;
+    case UGEMM_CONV_Y: *ptr = L.y; n = size_t(L.d.cout) * L.n; break;
+    case UGEMM_CONV_COL: *ptr = L.col; n = size_t(L.kdim) * L.n; break;
+    case UGEMM_CONV_DW: *ptr = L.dw; n = size_t(L.d.cout) * L.kdim; break;
+    case UGEMM_CONV_DCOL: *ptr = L.dcol; n = size_t(L.kdim) * L.n; break;
+    case UGEMM_CONV_DX: *ptr = L.dx; n = x_n; break;
+    case UGEMM_CONV_DY:
+      *ptr = (layer + 1 < static_cast<int>(s->layers.size())) ? s->layers[layer + 1].dx : L.y;
+      n = size_t(L.d.cout) * L.n;
+      break;
+    default: return UGEMM_ERR_ARG;
+  }
+  if (count) *count = n;
+  return UGEMM_OK;
+}
+
+UGEMM_API int ugemm_conv_stack_run(ugemm_conv_stack* s, int what, void* stream) {
+  if (!s || what < 1 || what > 3) return UGEMM_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (s->exec[what]) {
+    return cudaGraphLaunch(s->exec[what], st) == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+  }
+  return run_stack(s, what, st);
+}
+
+UGEMM_API double ugemm_conv_stack_flops(const ugemm_conv_stack* s, int what) {
+  if (!s) return 0;
+  return ((what & UGEMM_CONV_FORWARD) ? s->flops_fwd : 0) +
+         ((what & UGEMM_CONV_BACKWARD) ? s->flops_bwd : 0);
+}
+
+UGEMM_API int ugemm_conv_stack_destroy(ugemm_conv_stack* s) {
+  if (!s) return UGEMM_OK;
+  cudaDeviceSynchronize();
+  destroy_stack(s);
+  return UGEMM_OK;
+}
+
+}  // extern "C"
