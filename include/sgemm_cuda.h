@@ -109,6 +109,26 @@ UGEMM_API int ugemm_sgemm_dev(char major, char transa, char transb, int M, int N
                     const float *A, int lda, const float *B, int ldb, float beta, float *C,
                     int ldc, int precision, void *stream);
 
+/* Allocation-free variant of ugemm_sgemm_dev for the split-precision forms
+ * (UGEMM_PREC_AUTO, BF16X6, BF16X9, BF16X3).  It has no counterpart in the
+ * reference.  It is for callers that must not allocate device memory while
+ * they run -- a process whose device-memory budget is fixed at start-up, a
+ * framework whose own allocator owns all device memory, a latency-critical
+ * loop where an allocation could stall or fail -- and it calls no
+ * cudaMalloc, cudaFree or allocating routine.  The split pieces of A and B
+ * live in a fixed 64 MiB array in the library's device memory, held by every
+ * GPU that loads the library until the process exits; calls whose scratch
+ * (6 * (M + N) * roundup(K, 32) bytes for the three-piece forms) exceeds it
+ * return UGEMM_ERR_ARENA_TOO_SMALL.  The first call on a device looks up the
+ * array's device address (with that device current); make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other streams or host threads) race on it.  Device pointers,
+ * stream-ordered, same arguments as ugemm_sgemm_dev. */
+UGEMM_API int ugemm_sgemm_dev_noalloc(char major, char transa, char transb, int M, int N, int K,
+                                      float alpha, const float *A, int lda, const float *B,
+                                      int ldb, float beta, float *C, int ldc, int precision,
+                                      void *stream);
+
 /* Scratch bytes ugemm_sgemm_dev needs for this call (0 for most SIMT calls). */
 UGEMM_API size_t ugemm_workspace_bytes(char major, char transa, char transb, int M, int N, int K,
                              int lda, int ldb, int precision);
