@@ -168,6 +168,42 @@ def grouped_forms(ug, torch, stream, steps):
     return out
 
 
+def profile_case(args):
+    """One kernel family on a size ncu can capture (no timing, no JSON line):
+    'split'/'simt' = size^3 NN SGEMM; 'grouped_*' = the 256-problem group."""
+    import torch
+
+    import ugemm_gb300 as ug
+    from ugemm_gb300 import workloads
+    ug.build()
+    ug.load()
+    n = args.size
+    reps = max(1, args.steps)
+    if args.profile_case in ("split", "simt"):
+        A = torch.rand((n, n), device="cuda") * 2 - 1
+        B = torch.rand((n, n), device="cuda") * 2 - 1
+        C = torch.zeros((n, n), device="cuda")
+        prec = "bf16x6" if args.profile_case == "split" else "simt"
+        for _ in range(reps):
+            ug.sgemm_dev("N", "N", n, n, n, 1.0, A, n, B, n, 0.0, C, n, precision=prec)
+    else:
+        specs = []
+        for (ta, tb, M, N, K) in workloads.grouped_shapes():
+            A = torch.rand((M, K) if ta == "N" else (K, M), device="cuda") * 2 - 1
+            B = torch.rand((K, N) if tb == "N" else (N, K), device="cuda") * 2 - 1
+            C = torch.zeros((M, N), device="cuda")
+            specs.append(dict(ta=ta, tb=tb, M=M, N=N, K=K, alpha=1.0, beta=0.0, A=A,
+                              lda=A.stride(0), B=B, ldb=B.stride(0), C=C, ldc=N))
+        prec = "bf16x6" if args.profile_case == "grouped_split" else "simt"
+        plan = ug.GroupedPlan(specs, precision=prec)
+        for _ in range(reps):
+            plan.run()
+        plan.check()
+        plan.close()
+    torch.cuda.synchronize()
+    print(f"profile case {args.profile_case} size {n}: {reps} runs done")
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -196,9 +232,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile-case", default=None,
+                    choices=["split", "simt", "grouped_split", "grouped_simt"],
+                    help="run only this case --steps times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_case:
+        profile_case(args)
         return
 
     import numpy as np
