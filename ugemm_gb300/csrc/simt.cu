@@ -291,13 +291,18 @@ __global__ void __launch_bounds__(kThreads, 1)
 // src[r*sr + k*sk]) into a k-contiguous FP32 matrix dst[rows][ld], 32 x 64
 // tiles through shared memory so both source layouts read coalesced.
 __global__ void __launch_bounds__(256) pack_kmajor_batched_kernel(const PackJob* __restrict__ jobs,
-                                                                  int njobs) {
+                                                                  int njobs, int total_tiles) {
   __shared__ float tile[32][65];
+  __shared__ int starts[2048];
+  const int cached = min(njobs, 2048);
+  for (int i = threadIdx.x; i < cached; i += blockDim.x) starts[i] = jobs[i].tile_start;
+  __syncthreads();
+  for (int b = blockIdx.x; b < total_tiles; b += gridDim.x) {
   int lo = 0, hi = njobs - 1;
-  const int b = blockIdx.x;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
+    const int st = njobs <= 2048 ? starts[mid] : jobs[mid].tile_start;
+    if (st <= b) lo = mid; else hi = mid - 1;
   }
   const PackJob j = jobs[lo];
   const int local = b - j.tile_start;
@@ -327,6 +332,8 @@ __global__ void __launch_bounds__(256) pack_kmajor_batched_kernel(const PackJob*
       const int rr = (t >> 6) + 4 * i, r = r0 + rr;
       if (r < j.rows) j.dst[static_cast<size_t>(r) * j.ld + k] = tile[rr][t & 63];
     }
+  }
+  __syncthreads();  // the tile buffer is refilled by the next iteration
   }
 }
 
@@ -514,8 +521,12 @@ ugemm_status simt_grouped_launch(int tile, const CUtensorMap* maps, const SimtPr
 
 ugemm_status pack_batched_launch(const PackJob* jobs, int njobs, int total_tiles, cudaStream_t st) {
   if (total_tiles <= 0) return UGEMM_OK;
+  int sms = 148, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   prof_begin(st);
-  pack_kmajor_batched_kernel<<<total_tiles, 256, 0, st>>>(jobs, njobs);
+  pack_kmajor_batched_kernel<<<std::min(total_tiles, sms * 8), 256, 0, st>>>(jobs, njobs,
+                                                                             total_tiles);
   prof_end(st, kProfSplitPrep);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }

@@ -106,11 +106,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint8_t* smem = align1024(smem_raw);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S::STAGES * S::STAGE_BYTES);
   uint64_t* empty = full + S::STAGES;
+  // one set per TMEM accumulator buffer (two when 2 x 2 x BN columns fit)
+  constexpr int NB = S::ACC_BUFS;
   uint64_t* main_full = empty + S::STAGES;   // a main-product chunk is complete
-  uint64_t* main_empty = main_full + 1;      // the epilogue drained it
-  uint64_t* tile_full = main_empty + 1;      // all MMAs of a tile are complete
-  uint64_t* tmem_empty = tile_full + 1;      // the epilogue read both accumulators
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tmem_empty + 1);
+  uint64_t* main_empty = main_full + NB;     // the epilogue drained it
+  uint64_t* tile_full = main_empty + NB;     // all MMAs of a tile are complete
+  uint64_t* tmem_empty = tile_full + NB;     // the epilogue read both accumulators
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tmem_empty + NB);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -118,10 +120,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(main_full, 1);
-    mbar_init(main_empty, kTcEpiWarps);
-    mbar_init(tile_full, 1);
-    mbar_init(tmem_empty, kTcEpiWarps);
+    for (int b = 0; b < NB; ++b) {
+      mbar_init(&main_full[b], 1);
+      mbar_init(&main_empty[b], kTcEpiWarps);
+      mbar_init(&tile_full[b], 1);
+      mbar_init(&tmem_empty[b], kTcEpiWarps);
+    }
     fence_barrier_init();
   }
   if (warp == 1) {
@@ -171,13 +175,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = umma_idesc(1, 1, kTcBM, BN);
       const uint32_t base = smem_u32(smem);
-      const uint32_t t_main = tmem, t_corr = tmem + BN;
-      uint32_t it = 0, nbound = 0, ntile = 0;
+      uint32_t it = 0, ntile = 0;
+      uint32_t nbound[NB] = {};
       bool ok = true;
       for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
         TcProblem P;
         tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
-        if (ntile > 0 && !mbar_wait(tmem_empty, (ntile - 1) & 1, err, kDevTimeoutAccum)) {
+        const uint32_t buf = ntile % NB, use = ntile / NB;
+        const uint32_t t_main = tmem + buf * 2 * BN, t_corr = t_main + BN;
+        // the epilogue must have read this buffer's previous tile
+        if (use > 0 && !mbar_wait(&tmem_empty[buf], (use - 1) & 1, err, kDevTimeoutAccum)) {
           ok = false;
           break;
         }
@@ -202,8 +209,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           // main product; a new chunk restarts the accumulator once drained
           const bool chunk_start = (kb % chunk_kb) == 0;
           if (chunk_start && kb > 0) {
-            if (!mbar_wait(main_empty, nbound & 1, err, kDevTimeoutAccum)) { ok = false; break; }
-            ++nbound;
+            if (!mbar_wait(&main_empty[buf], nbound[buf] & 1, err, kDevTimeoutAccum)) {
+              ok = false;
+              break;
+            }
+            ++nbound[buf];
             tc_fence_after();
           }
 #pragma unroll
@@ -211,9 +221,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             umma_bf16(t_main, umma_smem_desc(sa + kk * 32, 512, 4),
                       umma_smem_desc(sb + kk * 32, 512, 4), idesc, !(chunk_start && kk == 0));
           umma_commit(&empty[s]);
-          if ((kb + 1) % chunk_kb == 0 && kb + 1 < P.nkb) umma_commit(main_full);
+          if ((kb + 1) % chunk_kb == 0 && kb + 1 < P.nkb) umma_commit(&main_full[buf]);
         }
-        umma_commit(tile_full);
+        umma_commit(&tile_full[buf]);
       }
     }
     __syncwarp();
@@ -224,36 +234,41 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int q = warp & 3;       // TMEM lane quarter this warp may access
     const int col_off = (ew >> 2) * HALF;
     const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
-    uint32_t nbound = 0, ntile = 0;
+    uint32_t ntile = 0;
+    uint32_t nbound[NB] = {};
     bool ok = true;
     for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
       TcProblem P;
       const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+      const uint32_t buf = ntile % NB, use = ntile / NB;
+      const uint32_t t_buf = tmem + buf * 2 * BN + lane_base + col_off;
       float acc[HALF];
 #pragma unroll
       for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
       const int nchunks = (P.nkb + chunk_kb - 1) / chunk_kb;
       for (int c = 0; c + 1 < nchunks; ++c) {
-        if (!__all_sync(0xffffffffu, mbar_wait(main_full, nbound & 1, err, kDevTimeoutAccum))) {
+        if (!__all_sync(0xffffffffu,
+                        mbar_wait(&main_full[buf], nbound[buf] & 1, err, kDevTimeoutAccum))) {
           ok = false;
           break;
         }
-        ++nbound;
+        ++nbound[buf];
         tc_fence_after();
 #pragma unroll
         for (int c32 = 0; c32 < HALF / 32; ++c32) {
           uint32_t r[32];
-          tmem_ld_32x32b_x32(tmem + lane_base + col_off + c32 * 32, r);
+          tmem_ld_32x32b_x32(t_buf + c32 * 32, r);
           tmem_ld_wait();
 #pragma unroll
           for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(main_empty);
+        if (lane == 0) mbar_arrive(&main_empty[buf]);
       }
       if (!ok) break;
-      if (!__all_sync(0xffffffffu, mbar_wait(tile_full, ntile & 1, err, kDevTimeoutAccum))) break;
+      if (!__all_sync(0xffffffffu, mbar_wait(&tile_full[buf], use & 1, err, kDevTimeoutAccum)))
+        break;
       tc_fence_after();
       // last main chunk, then the corrections (one 32-column slice live at a time)
 #pragma unroll
@@ -261,7 +276,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
         for (int c32 = 0; c32 < HALF / 32; ++c32) {
           uint32_t r[32];
-          tmem_ld_32x32b_x32(tmem + lane_base + part * BN + col_off + c32 * 32, r);
+          tmem_ld_32x32b_x32(t_buf + part * BN + c32 * 32, r);
           tmem_ld_wait();
 #pragma unroll
           for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
@@ -269,7 +284,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(tmem_empty);
+      if (lane == 0) mbar_arrive(&tmem_empty[buf]);
       // alpha/beta epilogue straight from registers (C not read when beta == 0)
       const int row = tc.m0 + q * 32 + lane;
       if (row < P.M) {
@@ -373,22 +388,47 @@ __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restri
   split_tile<NP>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile);
 }
 
-// Many operands in one launch: block b works on the job owning tile b.
-template <int NP>
-__global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
-                                                                   int njobs) {
-  __shared__ float tile[32][65];
-  int lo = 0, hi = njobs - 1;
-  const int b = blockIdx.x;
+// Many operands in one launch.  Blocks walk the tiles grid-stride; the
+// jobs' first-tile indices are cached in shared memory so finding the job of
+// a tile is a search in shared memory, not a chain of dependent global loads.
+constexpr int kJobCache = 2048;
+
+__device__ __forceinline__ int find_job(const int* starts, int n, int b) {
+  int lo = 0, hi = n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
+    if (starts[mid] <= b) lo = mid; else hi = mid - 1;
   }
-  const SplitJob j = jobs[lo];
-  const int local = b - j.tile_start;
-  const int tiles_k = (j.Kp + 63) / 64;
-  split_tile<NP>(j.src, j.sr, j.sk, j.rows, j.K, j.Kp, j.dst, (local / tiles_k) * 32,
-                 (local % tiles_k) * 64, tile);
+  return lo;
+}
+
+template <int NP>
+__global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
+                                                                   int njobs, int total_tiles) {
+  __shared__ float tile[32][65];
+  __shared__ int starts[kJobCache];
+  const int cached = min(njobs, kJobCache);
+  for (int i = threadIdx.x; i < cached; i += blockDim.x) starts[i] = jobs[i].tile_start;
+  __syncthreads();
+  for (int b = blockIdx.x; b < total_tiles; b += gridDim.x) {
+    int j;
+    if (njobs <= kJobCache) {
+      j = find_job(starts, njobs, b);
+    } else {
+      int lo = 0, hi = njobs - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
+      }
+      j = lo;
+    }
+    const SplitJob jb = jobs[j];
+    const int local = b - jb.tile_start;
+    const int tiles_k = (jb.Kp + 63) / 64;
+    split_tile<NP>(jb.src, jb.sr, jb.sk, jb.rows, jb.K, jb.Kp, jb.dst, (local / tiles_k) * 32,
+                   (local % tiles_k) * 64, tile);
+    __syncthreads();  // the tile buffer is refilled by the next iteration
+  }
 }
 
 template <int NP>
@@ -550,9 +590,10 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st) {
   if (total_tiles <= 0) return UGEMM_OK;
+  const int grid = std::min(total_tiles, sm_count() * 8);
   prof_begin(st);
-  if (pieces == 3) split_pieces_batched_kernel<3><<<total_tiles, 256, 0, st>>>(jobs, njobs);
-  else split_pieces_batched_kernel<2><<<total_tiles, 256, 0, st>>>(jobs, njobs);
+  if (pieces == 3) split_pieces_batched_kernel<3><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  else split_pieces_batched_kernel<2><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
   prof_end(st, kProfSplitPrep);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }

@@ -24,7 +24,9 @@ struct TcShape {
   static constexpr int FIT = (224 * 1024) / STAGE_BYTES;
   static constexpr int STAGES = FIT > 4 ? 4 : FIT;
   static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
-  static constexpr uint32_t TMEM_COLS = 2 * BN;  // main + correction accumulators
+  // main + correction accumulators, double-buffered across tiles when they fit
+  static constexpr int ACC_BUFS = (4 * BN <= 512) ? 2 : 1;
+  static constexpr uint32_t TMEM_COLS = ACC_BUFS * 2 * BN;
   static_assert(STAGES >= 2, "pipeline needs two stages");
   static_assert(SMEM <= 232448, "shared memory budget");
 };
