@@ -37,7 +37,16 @@ struct Scratch {
 };
 
 // Tile configurations of the SIMT kernel (rows x cols of C per CTA).
-enum SimtTile : int { kSimt128x128 = 0, kSimt64x64 = 1, kSimtTileCount = 2 };
+// 128x128 and 64x64 use 8 compute warps plus a TMA producer warp; the "np"
+// configurations drop the producer warp (thread 0 issues the copies), which
+// lifts the per-thread register limit from 168 to 255.
+enum SimtTile : int {
+  kSimt128x128 = 0,
+  kSimt64x64 = 1,
+  kSimt128x256 = 2,    // 8 x 16 per thread, producer-less
+  kSimt128x128np = 3,  // 8 x 8 per thread, producer-less
+  kSimtTileCount = 4
+};
 
 // Split-precision tensor-core variants.
 struct SplitPlan {

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "internal.h"
 #include "ptx.cuh"
@@ -105,6 +106,63 @@ __device__ __forceinline__ bool simt_mainloop(const uint8_t* smem, uint64_t* ful
     if (lane == 0) mbar_arrive(&empty[s]);
   }
   return true;
+}
+
+// One k-slice (kBK deep) of the register-blocked product, consumed from a
+// staged tile pair.  k-contiguous operands are read as float4 of 4 k; the
+// other layout is read per k so only TN (or TM) values are live at a time.
+template <int TM, int TN, bool AK, bool BKM>
+__device__ __forceinline__ void simt_consume(const float* As, const float* Bs, float (&acc)[TM][TN]) {
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;
+#pragma unroll
+  for (int q = 0; q < kBK / 4; ++q) {
+    float a[TM][4], bq[BKM ? TN : 1][4];
+    if (AK) {
+#pragma unroll
+      for (int i = 0; i < TM; ++i) {
+        const int r = ty + 16 * i;
+        const float4 v = *reinterpret_cast<const float4*>(As + r * kBK + 4 * sw64_chunk(r, q));
+        a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
+      }
+    }
+    if (BKM) {
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const int c = tx + 16 * j;
+        const float4 v = *reinterpret_cast<const float4*>(Bs + c * kBK + 4 * sw64_chunk(c, q));
+        bq[j][0] = v.x; bq[j][1] = v.y; bq[j][2] = v.z; bq[j][3] = v.w;
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      float av[TM], bv[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) av[i] = AK ? a[i][kk] : 0.f;
+      if (!AK) {
+#pragma unroll
+        for (int g = 0; g < TM / 4; ++g) {
+          const float4 v = *reinterpret_cast<const float4*>(As + (4 * q + kk) * BM + 64 * g + 4 * ty);
+          av[4 * g] = v.x; av[4 * g + 1] = v.y; av[4 * g + 2] = v.z; av[4 * g + 3] = v.w;
+        }
+      }
+      if (BKM) {
+#pragma unroll
+        for (int j = 0; j < TN; ++j) bv[j] = bq[j][kk];
+      } else {
+#pragma unroll
+        for (int g = 0; g < TN / 4; ++g) {
+          const float4 v = *reinterpret_cast<const float4*>(Bs + (4 * q + kk) * BN + 64 * g + 4 * tx);
+          bv[4 * g] = v.x; bv[4 * g + 1] = v.y; bv[4 * g + 2] = v.z; bv[4 * g + 3] = v.w;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+  }
 }
 
 // alpha/beta epilogue of one tile from registers; C is not read when beta == 0.
@@ -212,6 +270,73 @@ __global__ void __launch_bounds__(kThreads, 1)
   float acc[TM][TN];
   uint32_t it = 0;
   if (!simt_mainloop<TM, TN, AK, BKM>(smem, full, empty, nkt, it, acc, err)) return;
+  simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0);
+}
+
+// Producer-less variant: 8 warps only.  With no ninth warp every thread may
+// hold up to 255 registers (a ninth warp caps each scheduler's share at 168),
+// room for the 8 x 16 register block that halves shared-memory wavefronts per
+// FMA.  Thread 0 issues the TMA for stage kt + S - 1 once all warps released
+// the stage they consumed at kt - 1.
+template <int TM, int TN, bool AK, bool BKM>
+__global__ void __launch_bounds__(kConsumerWarps * 32, 1)
+    simt_sgemm_np_kernel(const __grid_constant__ CUtensorMap tmA,
+                         const __grid_constant__ CUtensorMap tmB, float* __restrict__ C, int M,
+                         int N, int K, int ldc, float alpha, float beta, int tiles_m, int tiles_n,
+                         int* err) {
+  using S = SimtShape<TM, TN>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::STAGE_BYTES);
+  uint64_t* empty = full + kStages;
+  int tile_m, tile_n;
+  raster_tile(blockIdx.x, tiles_m, tiles_n, tile_m, tile_n);
+  const int m0 = tile_m * S::BM, n0 = tile_n * S::BN;
+  const int nkt = (K + kBK - 1) / kBK;
+  const int tid = threadIdx.x, lane = tid & 31;
+  auto issue = [&](int kt) {
+    const int s = kt % kStages;
+    uint8_t* sa = smem + s * S::STAGE_BYTES;
+    uint8_t* sb = sa + S::A_BYTES;
+    mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
+    if (AK) tma_load_2d(sa, &tmA, &full[s], kt * kBK, m0);
+    else    tma_load_2d(sa, &tmA, &full[s], m0, kt * kBK);
+    if (BKM) tma_load_2d(sb, &tmB, &full[s], kt * kBK, n0);
+    else     tma_load_2d(sb, &tmB, &full[s], n0, kt * kBK);
+  };
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    fence_barrier_init();
+    tma_prefetch_desc(&tmA);
+    tma_prefetch_desc(&tmB);
+    for (int kt = 0; kt < min(kStages - 1, nkt); ++kt) issue(kt);  // first use of each stage
+  }
+  __syncthreads();
+  float acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+  for (int kt = 0; kt < nkt; ++kt) {
+    if (tid == 0) {
+      const int kn = kt + kStages - 1;
+      if (kn < nkt) {
+        if (!mbar_wait(&empty[kn % kStages], ((kn / kStages) & 1) ^ 1, err, kDevTimeoutEmpty))
+          return;
+        issue(kn);
+      }
+    }
+    const int s = kt % kStages;
+    if (!mbar_wait(&full[s], (kt / kStages) & 1, err, kDevTimeoutFull)) return;
+    const float* As = reinterpret_cast<const float*>(smem + s * S::STAGE_BYTES);
+    const float* Bs = reinterpret_cast<const float*>(smem + s * S::STAGE_BYTES + S::A_BYTES);
+    simt_consume<TM, TN, AK, BKM>(As, Bs, acc);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
   simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0);
 }
 
@@ -370,7 +495,7 @@ void stored_b(const Gemm& g, int& rows, int& cols) {
   if (g.tb == 'N') { rows = g.K; cols = g.N; } else { rows = g.N; cols = g.K; }
 }
 
-template <int TM, int TN, bool AK, bool BKM>
+template <int TM, int TN, bool AK, bool BKM, bool NP>
 ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, int ldb,
                       int* dev_err, cudaStream_t st) {
   using S = SimtShape<TM, TN>;
@@ -386,7 +511,8 @@ ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, in
   else     ok = encode_tmap_2d(&tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, B, g.N, g.K, ldb * 4ull,
                                S::BN, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
   if (!ok) return UGEMM_ERR_CUDA;
-  auto kern = simt_sgemm_kernel<TM, TN, AK, BKM>;
+  auto kern = NP ? simt_sgemm_np_kernel<TM, TN, AK, BKM> : simt_sgemm_kernel<TM, TN, AK, BKM>;
+  const int threads = NP ? kConsumerWarps * 32 : kThreads;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -396,20 +522,20 @@ ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, in
   }
   const int tiles_m = cdiv(g.M, S::BM), tiles_n = cdiv(g.N, S::BN);
   prof_begin(st);
-  kern<<<tiles_m * tiles_n, kThreads, S::SMEM, st>>>(ta, tb, g.C, g.M, g.N, g.K, g.ldc, g.alpha,
-                                                      g.beta, tiles_m, tiles_n, dev_err);
+  kern<<<tiles_m * tiles_n, threads, S::SMEM, st>>>(ta, tb, g.C, g.M, g.N, g.K, g.ldc, g.alpha,
+                                                     g.beta, tiles_m, tiles_n, dev_err);
   prof_end(st, kProfSimt);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
 
-template <int TM, int TN>
+template <int TM, int TN, bool NP>
 ugemm_status launch_tile(const Gemm& g, const float* A, int lda, const float* B, int ldb,
                          int* dev_err, cudaStream_t st) {
   const bool ak = g.ta == 'N', bk = g.tb == 'T';
-  if (ak && !bk) return launch_t<TM, TN, true, false>(g, A, lda, B, ldb, dev_err, st);
-  if (ak && bk) return launch_t<TM, TN, true, true>(g, A, lda, B, ldb, dev_err, st);
-  if (!ak && !bk) return launch_t<TM, TN, false, false>(g, A, lda, B, ldb, dev_err, st);
-  return launch_t<TM, TN, false, true>(g, A, lda, B, ldb, dev_err, st);
+  if (ak && !bk) return launch_t<TM, TN, true, false, NP>(g, A, lda, B, ldb, dev_err, st);
+  if (ak && bk) return launch_t<TM, TN, true, true, NP>(g, A, lda, B, ldb, dev_err, st);
+  if (!ak && !bk) return launch_t<TM, TN, false, false, NP>(g, A, lda, B, ldb, dev_err, st);
+  return launch_t<TM, TN, false, true, NP>(g, A, lda, B, ldb, dev_err, st);
 }
 
 }  // namespace
@@ -427,6 +553,13 @@ int simt_pick_tile(const Gemm& g) {
   int dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  static int forced = -2;
+  if (forced == -2) {
+    const char* e = std::getenv("UGEMM_SIMT_TILE");
+    forced = e ? std::atoi(e) : -1;
+    if (forced >= kSimtTileCount) forced = -1;
+  }
+  if (forced >= 0) return forced;
   const long big = long(cdiv(g.M, 128)) * cdiv(g.N, 128);
   return big >= 2L * sms ? kSimt128x128 : kSimt64x64;
 }
@@ -462,8 +595,12 @@ ugemm_status simt_launch(const Gemm& g, int tile, Scratch ws, int* dev_err, cuda
     prof_end(st, kProfAux);
     B = dst; ldb = ld; used += need;
   }
-  if (tile == kSimt64x64) return launch_tile<4, 4>(g, A, lda, B, ldb, dev_err, st);
-  return launch_tile<8, 8>(g, A, lda, B, ldb, dev_err, st);
+  switch (tile) {
+    case kSimt64x64: return launch_tile<4, 4, false>(g, A, lda, B, ldb, dev_err, st);
+    case kSimt128x256: return launch_tile<8, 16, true>(g, A, lda, B, ldb, dev_err, st);
+    case kSimt128x128np: return launch_tile<8, 8, true>(g, A, lda, B, ldb, dev_err, st);
+    default: return launch_tile<8, 8, false>(g, A, lda, B, ldb, dev_err, st);
+  }
 }
 
 ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st) {
