@@ -7,7 +7,7 @@
 //     persistent CTAs, which take tiles in round-robin order, meet the
 //     longest tiles first;
 //   * every operand gets a slot in one scratch buffer: bf16 pieces for the
-//     split-precision form, k-contiguous FP32 copies for the SIMT form;
+//     split-precision form, K x rows FP32 copies for the SIMT form;
 //   * one batched pre-pass launch writes all the slots, one persistent GEMM
 //     launch walks all output tiles of all problems; per-problem TMA
 //     descriptors and tile offsets live in one device table;
@@ -164,11 +164,12 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
     const Gemm& x = g[order[j]];
     a_off[j] = scratch;
     if (simt) {
-      ld_a[j] = static_cast<int>(align_up(std::max(x.K, 1), 4));
-      ld_b[j] = ld_a[j];
-      scratch += align_up(size_t(x.M) * ld_a[j] * 4, 256);
+      // packed K x M and K x N, rows padded to 16 bytes for TMA
+      ld_a[j] = static_cast<int>(align_up(x.M, 4));
+      ld_b[j] = static_cast<int>(align_up(x.N, 4));
+      scratch += align_up(size_t(std::max(x.K, 1)) * ld_a[j] * 4, 256);
       b_off[j] = scratch;
-      scratch += align_up(size_t(x.N) * ld_b[j] * 4, 256);
+      scratch += align_up(size_t(std::max(x.K, 1)) * ld_b[j] * 4, 256);
     } else {
       scratch += split_operand_bytes(pieces, x.M, x.K);
       b_off[j] = scratch;
@@ -206,8 +207,8 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
       prep += cdiv(x.M, 32) * tk;
       pjobs.push_back(PackJob{x.B, b_sr, b_sk, db, x.N, x.K, ld_b[j], prep});
       prep += cdiv(x.N, 32) * tk;
-      ok = simt_encode_kmajor(p->cfg.block_n == 64 ? kSimt64x64 : kSimt128x128, da, x.M, db, x.N,
-                              x.K, ld_a[j], ld_b[j], &maps[2 * j], &maps[2 * j + 1]);
+      ok = simt_encode_grouped(p->cfg.block_n == 64 ? kSimt64x64 : kSimt128x128, da, x.M, db,
+                               x.N, x.K, ld_a[j], ld_b[j], &maps[2 * j], &maps[2 * j + 1]);
       const int bm = p->cfg.block_n;
       SimtProblem sp{x.C, x.M, x.N, x.ldc, x.alpha, x.beta, cdiv(x.K, kBK), cdiv(x.M, bm),
                      cdiv(x.N, bm), tiles};

@@ -5,8 +5,8 @@
 // transpose pass (sgemm_ocl2.h:95-128, :180-199).  Here:
 //   * one CTA computes a BM x BN tile of C; 8 consumer warps (16 x 16 threads)
 //     each hold a TM x TN register block; a ninth warp is the TMA producer;
-//   * A and B k-slices (BK = 16) are staged by TMA into a 4-deep shared-memory
-//     ring guarded by mbarriers; k-contiguous tiles use the 64-byte swizzle
+//   * A and B k-slices (BK = 32) are staged by TMA into a 4-deep shared-memory
+//     ring guarded by mbarriers; k-contiguous tiles use the 128-byte swizzle
 //     so the float4 fragment reads are bank-conflict free;
 //   * transposed operands are handled by the tile layout (an m- or
 //     n-contiguous tile) -- no transpose kernel, no extra HBM pass;
@@ -31,9 +31,9 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-// Position of the 16-byte chunk `q` of row `r` in a 64-byte-row tile written
-// by TMA with CU_TENSOR_MAP_SWIZZLE_64B (address bits [4,6) ^= bits [7,9)).
-__device__ __forceinline__ int sw64_chunk(int r, int q) { return q ^ ((r >> 1) & 3); }
+// Position of the 16-byte chunk `q` of row `r` in a 128-byte-row tile written
+// by TMA with CU_TENSOR_MAP_SWIZZLE_128B (address bits [4,7) ^= bits [7,10)).
+__device__ __forceinline__ int swz_chunk(int r, int q) { return q ^ (r & 7); }
 
 // One BM x BN tile's k loop, consuming the TMA ring from stage counter `it`
 // (which keeps running across the tiles of a persistent CTA).  AK: op(A) rows
@@ -59,14 +59,14 @@ __device__ __forceinline__ bool simt_mainloop(const uint8_t* smem, uint64_t* ful
 #pragma unroll
     for (int q = 0; q < kBK / 4; ++q) {
       float a[TM][4], bf[TN][4];
-      if (AK) {  // As[BM][16], 64-byte swizzled rows; thread rows ty + 16 i
+      if (AK) {  // As[BM][32], 128-byte swizzled rows; thread rows ty + 16 i
 #pragma unroll
         for (int i = 0; i < TM; ++i) {
           const int r = ty + 16 * i;
-          const float4 v = *reinterpret_cast<const float4*>(As + r * kBK + 4 * sw64_chunk(r, q));
+          const float4 v = *reinterpret_cast<const float4*>(As + r * kBK + 4 * swz_chunk(r, q));
           a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
         }
-      } else {   // As[16][BM]; thread rows 64 g + 4 ty + {0..3}
+      } else {   // As[32][BM]; thread rows 64 g + 4 ty + {0..3}
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
@@ -77,14 +77,14 @@ __device__ __forceinline__ bool simt_mainloop(const uint8_t* smem, uint64_t* ful
             a[4 * g + 2][kk] = v.z; a[4 * g + 3][kk] = v.w;
           }
       }
-      if (BKM) {  // Bs[BN][16], 64-byte swizzled rows; thread cols tx + 16 j
+      if (BKM) {  // Bs[BN][32], 128-byte swizzled rows; thread cols tx + 16 j
 #pragma unroll
         for (int j = 0; j < TN; ++j) {
           const int c = tx + 16 * j;
-          const float4 v = *reinterpret_cast<const float4*>(Bs + c * kBK + 4 * sw64_chunk(c, q));
+          const float4 v = *reinterpret_cast<const float4*>(Bs + c * kBK + 4 * swz_chunk(c, q));
           bf[j][0] = v.x; bf[j][1] = v.y; bf[j][2] = v.z; bf[j][3] = v.w;
         }
-      } else {    // Bs[16][BN]; thread cols 64 g + 4 tx + {0..3}
+      } else {    // Bs[32][BN]; thread cols 64 g + 4 tx + {0..3}
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
@@ -123,7 +123,7 @@ __device__ __forceinline__ void simt_consume(const float* As, const float* Bs, f
 #pragma unroll
       for (int i = 0; i < TM; ++i) {
         const int r = ty + 16 * i;
-        const float4 v = *reinterpret_cast<const float4*>(As + r * kBK + 4 * sw64_chunk(r, q));
+        const float4 v = *reinterpret_cast<const float4*>(As + r * kBK + 4 * swz_chunk(r, q));
         a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
       }
     }
@@ -131,7 +131,7 @@ __device__ __forceinline__ void simt_consume(const float* As, const float* Bs, f
 #pragma unroll
       for (int j = 0; j < TN; ++j) {
         const int c = tx + 16 * j;
-        const float4 v = *reinterpret_cast<const float4*>(Bs + c * kBK + 4 * sw64_chunk(c, q));
+        const float4 v = *reinterpret_cast<const float4*>(Bs + c * kBK + 4 * swz_chunk(c, q));
         bq[j][0] = v.x; bq[j][1] = v.y; bq[j][2] = v.z; bq[j][3] = v.w;
       }
     }
@@ -341,8 +341,9 @@ __global__ void __launch_bounds__(kConsumerWarps * 32, 1)
 }
 
 // Persistent grouped SIMT GEMM: one CTA per SM walks the tiles of all
-// problems.  Operands were packed k-contiguous (A as M x Kpad, B as N x Kpad)
-// by the batched pre-pass, so every problem uses the (AK, BKM) layout.
+// problems.  The batched pre-pass packed every operand row-contiguous per k
+// (A as K x M, B as K x N), the layout with 512-byte TMA rows that this kernel
+// reads fastest, so all problems use the (!AK, !BKM) path.
 template <int TM, int TN>
 __global__ void __launch_bounds__(kThreads, 1)
     simt_grouped_kernel(const CUtensorMap* __restrict__ maps, const SimtProblem* __restrict__ probs,
@@ -394,8 +395,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
           uint8_t* sa = smem + s * S::STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_2d(sa, ma, &full[s], kt * kBK, m0);
-          tma_load_2d(sa + S::A_BYTES, mb, &full[s], kt * kBK, n0);
+          tma_load_2d(sa, ma, &full[s], m0, kt * kBK);
+          tma_load_2d(sa + S::A_BYTES, mb, &full[s], n0, kt * kBK);
         }
       }
     }
@@ -407,14 +408,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     int p, m0, n0;
     locate(t, P, p, m0, n0);
     float acc[TM][TN];
-    if (!simt_mainloop<TM, TN, true, true>(smem, full, empty, P.nkt, it, acc, err)) return;
-    simt_store<TM, TN, true, true>(acc, P.C, P.M, P.N, P.ldc, P.alpha, P.beta, m0, n0);
+    if (!simt_mainloop<TM, TN, false, false>(smem, full, empty, P.nkt, it, acc, err)) return;
+    simt_store<TM, TN, false, false>(acc, P.C, P.M, P.N, P.ldc, P.alpha, P.beta, m0, n0);
   }
 }
 
 // Batched pre-pass of the grouped SIMT form: copy op(X) (element (r, k) at
-// src[r*sr + k*sk]) into a k-contiguous FP32 matrix dst[rows][ld], 32 x 64
-// tiles through shared memory so both source layouts read coalesced.
+// src[r*sr + k*sk]) to dst[k*ld + r] (rows contiguous per k), 32 x 64 tiles
+// through shared memory so both source layouts read and write coalesced.
 __global__ void __launch_bounds__(256) pack_kmajor_batched_kernel(const PackJob* __restrict__ jobs,
                                                                   int njobs, int total_tiles) {
   __shared__ float tile[32][65];
@@ -450,12 +451,12 @@ __global__ void __launch_bounds__(256) pack_kmajor_batched_kernel(const PackJob*
     }
   }
   __syncthreads();
-  const int k = k0 + (t & 63);
-  if (k < j.K) {
+  {
+    const int rr = t & 31, r = r0 + rr;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const int rr = (t >> 6) + 4 * i, r = r0 + rr;
-      if (r < j.rows) j.dst[static_cast<size_t>(r) * j.ld + k] = tile[rr][t & 63];
+      const int kk = (t >> 5) + 8 * i, k = k0 + kk;
+      if (r < j.rows && k < j.K) j.dst[static_cast<size_t>(k) * j.ld + r] = tile[rr][kk];
     }
   }
   __syncthreads();  // the tile buffer is refilled by the next iteration
@@ -502,16 +503,19 @@ ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, in
   CUtensorMap ta, tb;
   bool ok;
   if (AK) ok = encode_tmap_2d(&ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, A, g.K, g.M, lda * 4ull,
-                              kBK, S::BM, CU_TENSOR_MAP_SWIZZLE_64B);
+                              kBK, S::BM, CU_TENSOR_MAP_SWIZZLE_128B);
   else    ok = encode_tmap_2d(&ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, A, g.M, g.K, lda * 4ull,
                               S::BM, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
   if (!ok) return UGEMM_ERR_CUDA;
   if (BKM) ok = encode_tmap_2d(&tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, B, g.K, g.N, ldb * 4ull,
-                               kBK, S::BN, CU_TENSOR_MAP_SWIZZLE_64B);
+                               kBK, S::BN, CU_TENSOR_MAP_SWIZZLE_128B);
   else     ok = encode_tmap_2d(&tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, B, g.N, g.K, ldb * 4ull,
                                S::BN, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
   if (!ok) return UGEMM_ERR_CUDA;
-  auto kern = NP ? simt_sgemm_np_kernel<TM, TN, AK, BKM> : simt_sgemm_kernel<TM, TN, AK, BKM>;
+  void (*kern)(const CUtensorMap, const CUtensorMap, float*, int, int, int, int, float, float, int,
+               int, int*);
+  if constexpr (NP) kern = simt_sgemm_np_kernel<TM, TN, AK, BKM>;
+  else kern = simt_sgemm_kernel<TM, TN, AK, BKM>;
   const int threads = NP ? kConsumerWarps * 32 : kThreads;
   static bool attr_set = false;  // per instantiation
   if (!attr_set) {
@@ -615,13 +619,13 @@ ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st) {
 
 int simt_block(int tile) { return tile == kSimt64x64 ? 64 : 128; }
 
-bool simt_encode_kmajor(int tile, const float* a, int M, const float* b, int N, int K, int ld_a,
-                        int ld_b, CUtensorMap* ta, CUtensorMap* tb) {
+bool simt_encode_grouped(int tile, const float* a, int M, const float* b, int N, int K, int ld_a,
+                         int ld_b, CUtensorMap* ta, CUtensorMap* tb) {
   const int bm = simt_block(tile);
-  return encode_tmap_2d(ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a, std::max(K, 1), M, ld_a * 4ull,
-                        kBK, bm, CU_TENSOR_MAP_SWIZZLE_64B) &&
-         encode_tmap_2d(tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b, std::max(K, 1), N, ld_b * 4ull,
-                        kBK, bm, CU_TENSOR_MAP_SWIZZLE_64B);
+  return encode_tmap_2d(ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a, M, std::max(K, 1), ld_a * 4ull,
+                        bm, kBK, CU_TENSOR_MAP_SWIZZLE_NONE) &&
+         encode_tmap_2d(tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b, N, std::max(K, 1), ld_b * 4ull,
+                        bm, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
 }
 
 namespace {

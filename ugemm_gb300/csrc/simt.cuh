@@ -8,7 +8,7 @@
 
 namespace ugemm {
 
-constexpr int kBK = 16;            // k depth of one pipeline stage
+constexpr int kBK = 32;            // k depth of one pipeline stage (128-byte k rows)
 constexpr int kStages = 4;         // TMA ring depth
 constexpr int kConsumerWarps = 8;  // 16 x 16 compute threads
 constexpr int kThreads = (kConsumerWarps + 1) * 32;
@@ -34,7 +34,8 @@ struct SimtProblem {
   int tile_start;
 };
 
-// One operand of the batched FP32 pack (op(X) -> k-contiguous rows x ld).
+// One operand of the batched FP32 pack: op(X) (rows x K) -> dst[k][r] with
+// row length ld (rows contiguous, the layout the SIMT kernel reads fastest).
 struct PackJob {
   const float* src;
   long long sr, sk;
@@ -47,8 +48,8 @@ ugemm_status simt_grouped_launch(int tile, const CUtensorMap* maps, const SimtPr
                                  int nprob, int total_tiles, int max_ctas, int* dev_err,
                                  cudaStream_t st);
 ugemm_status pack_batched_launch(const PackJob* jobs, int njobs, int total_tiles, cudaStream_t st);
-bool simt_encode_kmajor(int tile, const float* a, int M, const float* b, int N, int K, int ld_a,
-                        int ld_b, CUtensorMap* ta, CUtensorMap* tb);
+bool simt_encode_grouped(int tile, const float* a, int M, const float* b, int N, int K, int ld_a,
+                         int ld_b, CUtensorMap* ta, CUtensorMap* tb);
 int simt_block(int tile);
 
 }  // namespace ugemm

@@ -326,56 +326,82 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // ---------------------------------------------------------------- split pass
 // One 32-row x 64-k tile of op(X) (element (r, k) at src[r*sr + k*sk]) into
 // NP bf16 planes dst[p][rows][Kp], through shared memory so that both source
-// layouts are read coalesced.  Zero for k >= K.
+// layouts are read coalesced: float4 loads along the contiguous dimension
+// when the operand allows it, one 16-byte store of 8 k per plane per thread.
+// Zero for k >= K.
 template <int NP>
 __device__ __forceinline__ void split_tile(const float* __restrict__ src, long long sr,
                                            long long sk, int rows, int K, int Kp,
                                            __nv_bfloat16* __restrict__ dst, int r0, int k0,
                                            float (*tile)[65]) {
   const int t = threadIdx.x;
-  if (sk == 1) {
-    const int k = k0 + (t & 63);
+  const bool kcontig = sk == 1;
+  const long long other = kcontig ? sr : sk;
+  const bool vec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) && ((other & 3) == 0);
+  if (kcontig) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int rr = (t >> 6) + 4 * i, r = r0 + rr;
-      tile[rr][t & 63] = (r < rows && k < K) ? src[r * sr + k] : 0.f;
+    for (int i = 0; i < 2; ++i) {
+      const int idx = t + 256 * i, rr = idx >> 4, c4 = (idx & 15) * 4;
+      const int r = r0 + rr, k = k0 + c4;
+      float v[4];
+      if (vec && r < rows && k + 3 < K) {
+        const float4 x = *reinterpret_cast<const float4*>(src + r * sr + k);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) v[e] = (r < rows && k + e < K) ? src[r * sr + k + e] : 0.f;
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) tile[rr][c4 + e] = v[e];
     }
   } else {
-    const int rr = t & 31, r = r0 + rr;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int kk = (t >> 5) + 8 * i, k = k0 + kk;
-      tile[rr][kk] = (r < rows && k < K) ? src[r * sr + k * sk] : 0.f;
+    for (int i = 0; i < 2; ++i) {
+      const int idx = t + 256 * i, kk = idx >> 3, q4 = (idx & 7) * 4;
+      const int r = r0 + q4, k = k0 + kk;
+      float v[4];
+      if (vec && r + 3 < rows && k < K) {
+        const float4 x = *reinterpret_cast<const float4*>(src + r + k * sk);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) v[e] = (r + e < rows && k < K) ? src[(r + e) * sr + k * sk] : 0.f;
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) tile[q4 + e][kk] = v[e];
     }
   }
   __syncthreads();
-  const int kp = t & 31;
-  const int k = k0 + 2 * kp;
-  if (k < Kp) {
+  const int rr = t >> 3, g8 = (t & 7) * 8;
+  const int r = r0 + rr, k = k0 + g8;
+  if (r < rows && k < Kp) {
     const size_t plane = static_cast<size_t>(rows) * Kp;
+    uint32_t packed[3][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int rr = (t >> 5) + 8 * i, r = r0 + rr;
-      if (r >= rows) continue;
+    for (int e = 0; e < 8; e += 2) {
       __nv_bfloat16 pc[3][2];
 #pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        float rem = tile[rr][2 * kp + e];
+      for (int h = 0; h < 2; ++h) {
+        float rem = tile[rr][g8 + e + h];
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-          pc[p][e] = __float2bfloat16_rn(rem);
-          rem = rem - __bfloat162float(pc[p][e]);
+          pc[p][h] = __float2bfloat16_rn(rem);
+          rem = rem - __bfloat162float(pc[p][h]);
         }
       }
-      const size_t off = static_cast<size_t>(r) * Kp + k;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {
-        __nv_bfloat162 v;
-        v.x = pc[p][0];
-        v.y = pc[p][1];
-        *reinterpret_cast<__nv_bfloat162*>(dst + p * plane + off) = v;
+        __nv_bfloat162 two;
+        two.x = pc[p][0];
+        two.y = pc[p][1];
+        packed[p][e / 2] = *reinterpret_cast<uint32_t*>(&two);
       }
     }
+    const size_t off = static_cast<size_t>(r) * Kp + k;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+      *reinterpret_cast<uint4*>(dst + p * plane + off) =
+          make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
   }
 }
 
