@@ -285,7 +285,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmem_empty[buf]);
-      // alpha/beta epilogue straight from registers (C not read when beta == 0)
+      // alpha/beta epilogue (C not read when beta == 0)
+      if constexpr (S::STAGE_C) {
+        // transpose each 32 x 32 block through shared memory: lane = column,
+        // one 128-byte row segment per store instruction
+        float* stage = reinterpret_cast<float*>(smem + S::STAGES * S::STAGE_BYTES + 256) +
+                       ew * 32 * 33;
+        const int col = tc.n0 + col_off + lane;
+#pragma unroll
+        for (int c32 = 0; c32 < HALF / 32; ++c32) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = acc[c32 * 32 + j];
+          __syncwarp();
+          const int cc = col + c32 * 32;
+          if (cc < P.N) {
+            for (int rr = 0; rr < 32; ++rr) {
+              const int row = tc.m0 + q * 32 + rr;
+              if (row >= P.M) break;
+              float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
+              float v = P.alpha * stage[rr * 33 + lane];
+              if (P.beta != 0.f) v += P.beta * *cp;
+              *cp = v;
+            }
+          }
+          __syncwarp();
+        }
+        continue;
+      }
       const int row = tc.m0 + q * 32 + lane;
       if (row < P.M) {
         float* crow = P.C + static_cast<size_t>(row) * P.ldc;

@@ -23,7 +23,12 @@ struct TcShape {
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr int FIT = (224 * 1024) / STAGE_BYTES;
   static constexpr int STAGES = FIT > 4 ? 4 : FIT;
-  static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
+  // 128-wide tiles stage each epilogue warp's 32 x 32 output block in shared
+  // memory (padded rows) so C is written row by row, coalesced; 256-wide
+  // tiles have no room left and store straight from registers.
+  static constexpr bool STAGE_C = (BN == 128);
+  static constexpr size_t STAGE_C_BYTES = STAGE_C ? size_t(kTcEpiWarps) * 32 * 33 * 4 : 0;
+  static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256 + STAGE_C_BYTES;
   // main + correction accumulators, double-buffered across tiles when they fit
   static constexpr int ACC_BUFS = (4 * BN <= 512) ? 2 : 1;
   static constexpr uint32_t TMEM_COLS = ACC_BUFS * 2 * BN;
