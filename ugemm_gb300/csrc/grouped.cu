@@ -139,6 +139,13 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
     p->cfg = *config;
   } else if (!tuned_config(count, problems, form, &p->cfg)) {
     p->cfg = default_grouped_config(form);
+    // Untuned split plans: 256-wide tiles only pay when the problems are wide
+    // (measured: 128 wins on the 256-problem set with N in [32, 1024]).
+    if (form != UGEMM_PREC_SIMT) {
+      double n_sum = 0;
+      for (const Gemm& x : g) n_sum += x.N;
+      if (n_sum / count < 512) p->cfg.block_n = 128;
+    }
   }
   if (form != UGEMM_PREC_SIMT) {
     if (p->cfg.block_n != 128 && p->cfg.block_n != 256) p->cfg.block_n = 256;

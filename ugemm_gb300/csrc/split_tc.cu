@@ -440,18 +440,120 @@ __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restri
   split_tile<NP>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile);
 }
 
-// Many operands in one launch.  Blocks walk the tiles grid-stride; the
-// jobs' first-tile indices are cached in shared memory so finding the job of
-// a tile is a search in shared memory, not a chain of dependent global loads.
+// Raw values of one 32 x 64 tile, read with the same float4 pattern as
+// split_tile, kept in registers so the next tile's loads overlap the current
+// tile's split and stores.
+struct RawTile {
+  float v[2][4];
+};
+
+__device__ __forceinline__ void load_raw(const SplitJob& j, int r0, int k0, RawTile& out) {
+  const int t = threadIdx.x;
+  const bool kcontig = j.sk == 1;
+  const long long other = kcontig ? j.sr : j.sk;
+  const bool vec = ((reinterpret_cast<uintptr_t>(j.src) & 15) == 0) && ((other & 3) == 0);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int idx = t + 256 * i;
+    if (kcontig) {
+      const int rr = idx >> 4, c4 = (idx & 15) * 4, r = r0 + rr, k = k0 + c4;
+      if (vec && r < j.rows && k + 3 < j.K) {
+        const float4 x = *reinterpret_cast<const float4*>(j.src + r * j.sr + k);
+        out.v[i][0] = x.x; out.v[i][1] = x.y; out.v[i][2] = x.z; out.v[i][3] = x.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          out.v[i][e] = (r < j.rows && k + e < j.K) ? j.src[r * j.sr + k + e] : 0.f;
+      }
+    } else {
+      const int kk = idx >> 3, q4 = (idx & 7) * 4, r = r0 + q4, k = k0 + kk;
+      if (vec && r + 3 < j.rows && k < j.K) {
+        const float4 x = *reinterpret_cast<const float4*>(j.src + r + k * j.sk);
+        out.v[i][0] = x.x; out.v[i][1] = x.y; out.v[i][2] = x.z; out.v[i][3] = x.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          out.v[i][e] = (r + e < j.rows && k < j.K) ? j.src[(r + e) * j.sr + k * j.sk] : 0.f;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void raw_to_smem(const SplitJob& j, const RawTile& in, float (*tile)[65]) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int idx = t + 256 * i;
+    if (j.sk == 1) {
+      const int rr = idx >> 4, c4 = (idx & 15) * 4;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) tile[rr][c4 + e] = in.v[i][e];
+    } else {
+      const int kk = idx >> 3, q4 = (idx & 7) * 4;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) tile[q4 + e][kk] = in.v[i][e];
+    }
+  }
+}
+
+// bf16 pieces of one tile from shared memory: 8 consecutive k of one row per
+// thread, one 16-byte store per plane.
+template <int NP>
+__device__ __forceinline__ void split_store(const SplitJob& j, int r0, int k0, float (*tile)[65]) {
+  const int t = threadIdx.x;
+  const int rr = t >> 3, g8 = (t & 7) * 8;
+  const int r = r0 + rr, k = k0 + g8;
+  if (r >= j.rows || k >= j.Kp) return;
+  const size_t plane = static_cast<size_t>(j.rows) * j.Kp;
+  uint32_t packed[3][4];
+#pragma unroll
+  for (int e = 0; e < 8; e += 2) {
+    __nv_bfloat16 pc[3][2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float rem = tile[rr][g8 + e + h];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        pc[p][h] = __float2bfloat16_rn(rem);
+        rem = rem - __bfloat162float(pc[p][h]);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      __nv_bfloat162 two;
+      two.x = pc[p][0];
+      two.y = pc[p][1];
+      packed[p][e / 2] = *reinterpret_cast<uint32_t*>(&two);
+    }
+  }
+  const size_t off = static_cast<size_t>(r) * j.Kp + k;
+#pragma unroll
+  for (int p = 0; p < NP; ++p)
+    *reinterpret_cast<uint4*>(j.dst + p * plane + off) =
+        make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+}
+
+// Many operands in one launch.  Blocks walk the tiles grid-stride; the next
+// tile's loads are issued before the current tile is split and stored, and
+// the jobs' first-tile indices are cached in shared memory so finding a
+// tile's job is a search in shared memory, not a chain of global loads.
 constexpr int kJobCache = 2048;
 
-__device__ __forceinline__ int find_job(const int* starts, int n, int b) {
+__device__ __forceinline__ int find_job(const int* starts, const SplitJob* jobs, int n, int b) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (starts[mid] <= b) lo = mid; else hi = mid - 1;
+    const int st = n <= kJobCache ? starts[mid] : jobs[mid].tile_start;
+    if (st <= b) lo = mid; else hi = mid - 1;
   }
   return lo;
+}
+
+__device__ __forceinline__ void tile_origin(const SplitJob& j, int b, int& r0, int& k0) {
+  const int local = b - j.tile_start;
+  const int tiles_k = (j.Kp + 63) / 64;
+  r0 = (local / tiles_k) * 32;
+  k0 = (local % tiles_k) * 64;
 }
 
 template <int NP>
@@ -462,24 +564,29 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
   const int cached = min(njobs, kJobCache);
   for (int i = threadIdx.x; i < cached; i += blockDim.x) starts[i] = jobs[i].tile_start;
   __syncthreads();
-  for (int b = blockIdx.x; b < total_tiles; b += gridDim.x) {
-    int j;
-    if (njobs <= kJobCache) {
-      j = find_job(starts, njobs, b);
-    } else {
-      int lo = 0, hi = njobs - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].tile_start <= b) lo = mid; else hi = mid - 1;
-      }
-      j = lo;
+  int b = blockIdx.x;
+  if (b >= total_tiles) return;
+  SplitJob cur = jobs[find_job(starts, jobs, njobs, b)];
+  int r0, k0;
+  tile_origin(cur, b, r0, k0);
+  RawTile raw;
+  load_raw(cur, r0, k0, raw);
+  for (; b < total_tiles; b += gridDim.x) {
+    raw_to_smem(cur, raw, tile);
+    const int nb = b + gridDim.x;
+    SplitJob nxt = cur;
+    int nr0 = 0, nk0 = 0;
+    if (nb < total_tiles) {  // next tile's loads in flight during this tile's stores
+      nxt = jobs[find_job(starts, jobs, njobs, nb)];
+      tile_origin(nxt, nb, nr0, nk0);
+      load_raw(nxt, nr0, nk0, raw);
     }
-    const SplitJob jb = jobs[j];
-    const int local = b - jb.tile_start;
-    const int tiles_k = (jb.Kp + 63) / 64;
-    split_tile<NP>(jb.src, jb.sr, jb.sk, jb.rows, jb.K, jb.Kp, jb.dst, (local / tiles_k) * 32,
-                   (local % tiles_k) * 64, tile);
-    __syncthreads();  // the tile buffer is refilled by the next iteration
+    __syncthreads();
+    split_store<NP>(cur, r0, k0, tile);
+    __syncthreads();
+    cur = nxt;
+    r0 = nr0;
+    k0 = nk0;
   }
 }
 
