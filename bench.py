@@ -61,7 +61,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -227,7 +227,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=8192)
@@ -372,11 +372,13 @@ def main():
     peak_split = pk["bf16_tflops"] / 6.0
     sm_max = pk.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-    traffic = None
+    traffic = None  # DRAM bytes per launch from the committed ncu capture
     try:
-        with open(os.path.join(ROOT, "profiles", "split_tc_traffic.json")) as f:
-            traffic = json.load(f).get("bytes_per_launch_8192")
-    except Exception:
+        with open(os.path.join(ROOT, "profiles", "split_tc_kernel_sgemm8192_traffic.md")) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_8192:") and n == 8192:
+                    traffic = int(line.split(":")[1])
+    except OSError:
         pass
 
     line = {
