@@ -212,6 +212,11 @@ ugemm_status host_gemm(const Gemm& g, int precision, void* arena, size_t arena_b
   const size_t b_bytes = align_up(b_rows * g.ldb * sizeof(float), 256);
   const size_t c_bytes = align_up(size_t(g.M) * g.ldc * sizeof(float), 256);
   const int form = resolve_form(precision, g);
+  {
+    ugemm_status ps = host_gemm_pipelined(g, form, arena, arena_bytes, d.dev_err, st);
+    if (ps == UGEMM_OK) return check_device_error(d, st);
+    if (ps != UGEMM_ERR_UNSUPPORTED) return fail(ps, "pipelined host GEMM failed%s");
+  }
   const bool need_ab = g.K > 0 && g.alpha != 0.f;
   const size_t need = (need_ab ? a_bytes + b_bytes : 0) + c_bytes + scratch_for(g, form);
   if (need > arena_bytes) return fail(UGEMM_ERR_ARENA_TOO_SMALL, "device arena too small for this call%s");

@@ -86,6 +86,12 @@ ugemm_tile_config default_grouped_config(int form);
 bool tuned_config(int count, const ugemm_problem* problems, int precision, ugemm_tile_config* cfg);
 int split_default_chunk_kb();
 
+// Host-pointer GEMM with overlapped copies (row bands of C); returns
+// UGEMM_ERR_UNSUPPORTED when the call is too small or the arena too tight,
+// in which case the caller runs the plain copy-compute-copy sequence.
+ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t arena_bytes,
+                                 int* dev_err, cudaStream_t caller);
+
 // Per-thread last error, shared by the void compat entry points.
 void set_last_error(ugemm_status s, const std::string& msg);
 

@@ -760,3 +760,30 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
 int split_kp(int K) { return kp_of(K); }
 
 }  // namespace ugemm
+
+namespace ugemm {
+
+// Split one operand (element (r, k) at src[r*sr + k*sk]) into `pieces` bf16
+// planes [pieces][rows][Kp] at dst.
+ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
+                                  int rows, int K, void* dst, cudaStream_t st) {
+  const int Kp = kp_of(K);
+  auto* d = static_cast<__nv_bfloat16*>(dst);
+  if (pieces == 3) launch_split<3>(src, sr, sk, rows, K, Kp, d, st);
+  else launch_split<2>(src, sr, sk, rows, K, Kp, d, st);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+// GEMM on pieces already split: C = alpha * A*B^T-pieces + beta * C.
+ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
+                                  const void* b_pieces, int* dev_err, cudaStream_t st) {
+  CUtensorMap ta, tb;
+  if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb))
+    return UGEMM_ERR_CUDA;
+  const TcProblem P = split_problem(g, p.block_n, 0);
+  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, 1, P.tiles_m * P.tiles_n, chunk, 0,
+                           dev_err, st);
+}
+
+}  // namespace ugemm

@@ -69,5 +69,9 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                int max_ctas, int* dev_err, cudaStream_t st);
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st);
+ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
+                                  int rows, int K, void* dst, cudaStream_t st);
+ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
+                                  const void* b_pieces, int* dev_err, cudaStream_t st);
 
 }  // namespace ugemm
