@@ -168,6 +168,74 @@ def grouped_forms(ug, torch, stream, steps):
     return out
 
 
+def backward_forms(ug, torch, stream, steps):
+    """Config 3: forward + hand-written adjoint (dA, dB) at 4096^3 and
+    2048 x 8192 x 1024, TFLOPS of the backward pair (4MNK) in both forms."""
+    out = {}
+    for (M, N, K) in ((4096, 4096, 4096), (2048, 8192, 1024)):
+        g = torch.Generator(device="cuda").manual_seed(SEED + M + N + K)
+        A = torch.rand((M, K), device="cuda", generator=g) * 2 - 1
+        B = torch.rand((K, N), device="cuda", generator=g) * 2 - 1
+        W = torch.randn((M, N), device="cuda", generator=g)
+        dA = torch.empty_like(A)
+        dB = torch.empty_like(B)
+        row = {}
+        for prec in ("bf16x6", "simt"):
+            def bwd():
+                ug.sgemm_backward("N", "N", M, N, K, 1.0, A, K, B, N, W, N, 0.0, dA, K, 0.0, dB, N,
+                                  precision=prec, stream=stream)
+            for _ in range(3):
+                bwd()
+            reps = max(5, steps // 10)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                bwd()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            ref_a = W.double() @ B.double().T
+            err = float(torch.linalg.norm(dA.double() - ref_a) / torch.linalg.norm(ref_a))
+            row[prec] = {"tflops": round(4.0 * M * N * K / (ms * 1e-3) / 1e12, 2),
+                         "ms": round(ms, 3), "dA_normwise_err_fp64": err}
+        out[f"{M}x{N}x{K}"] = row
+    return out
+
+
+def conv_forms(ug, torch, stream, steps):
+    """Config 5: the 12-layer im2col conv stack, forward + dX + dW as grouped
+    GEMMs replayed from one CUDA graph; TFLOPS over the GEMM flops."""
+    from ugemm_gb300 import workloads
+    batch = 32
+    layers = workloads.conv_layers(batch)
+    out = {"layers": len(layers), "batch": batch}
+    for prec in ("bf16x6", "simt"):
+        st = ug.ConvStack(layers, batch, precision=prec, graph=True)
+        g = torch.Generator(device="cuda").manual_seed(SEED + 5)
+        cin, _, h, w, _ = layers[0]
+        st.tensor(0, "x", (cin, batch * h * w)).copy_(
+            torch.rand((cin, batch * h * w), device="cuda", generator=g))
+        for l, (ci, co, _, _, _) in enumerate(layers):
+            st.tensor(l, "w", (co, ci * 9)).copy_(
+                torch.randn((co, ci * 9), device="cuda", generator=g) * (2.0 / (ci * 9)) ** 0.5)
+        for _ in range(2):
+            st.run(stream=stream)
+        reps = max(3, steps // 20)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            st.run(stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[prec] = {"tflops": round(st.flops() / (ms * 1e-3) / 1e12, 2), "ms": round(ms, 3),
+                     "gemm_gflop": round(st.flops() / 1e9, 1)}
+        st.close()
+    return out
+
+
 def profile_case(args):
     """One kernel family on a size ncu can capture (no timing, no JSON line):
     'split'/'simt' = size^3 NN SGEMM; 'grouped_*' = the 256-problem group."""
@@ -336,6 +404,8 @@ def main():
 
     # --- batching form: 256 uneven problems, one persistent launch, CUDA graph
     grouped = grouped_forms(ug, torch, stream, args.steps)
+    backward = backward_forms(ug, torch, stream, args.steps)
+    conv = conv_forms(ug, torch, stream, args.steps)
 
     # --- end to end through the reference-facing host API (sgemm_cuda)
     hA = A.cpu().pin_memory()
@@ -406,6 +476,8 @@ def main():
             "split_err_over_simt_err": round(err_split / err_simt, 4),
             "split_prepass_ms": round(prep_ms, 4), "split_gemm_ms": round(gemm_ms, 4),
             "grouped": grouped,
+            "backward": backward,
+            "conv_stack": conv,
         },
         "roofline": {"bound": "tensor", "achieved": round(achieved, 3),
                      "peak": round(peak_split, 3), "unit": "TFLOP/s",
