@@ -256,6 +256,21 @@ UGEMM_API int ugemm_conv_stack_run(ugemm_conv_stack *stack, int what, void *stre
 UGEMM_API double ugemm_conv_stack_flops(const ugemm_conv_stack *stack, int what);
 UGEMM_API int ugemm_conv_stack_destroy(ugemm_conv_stack *stack);
 
+/* ------------------------------------------------------------------ */
+/* Level-1/2 helpers of ugemm.h, on device pointers (stream-ordered).  */
+/* ------------------------------------------------------------------ */
+/* saxpy_cpu (ugemm.h:86-97): y[i*incy] += alpha * x[i*incx], i < N. */
+UGEMM_API int ugemm_saxpy(int N, float alpha, const float *x, int incx, float *y, int incy,
+                          void *stream);
+/* sgemv_cpu (ugemm.h:129-160), column-major A: trans 'N': A is M x N,
+ * y = alpha*A*x + beta*y; trans 'T': A is N x M, y = alpha*A^T*x + beta*y
+ * (y has M entries, x has N in both cases, as in the reference).  x is read
+ * with stride incx (the reference reads x with incy; the two agree whenever
+ * incx == incy); beta == 0 means y is not read. */
+UGEMM_API int ugemm_sgemv(char trans, int M, int N, float alpha, const float *A, int lda,
+                          const float *x, int incx, float beta, float *y, int incy,
+                          void *stream);
+
 /* Per-kernel timing for benchmarks (no reference counterpart; the reference's
  * oclTime at ocl.h:344-352 is never enabled).  While enabled, each library
  * kernel launch is bracketed by CUDA events on its own stream.  collect()

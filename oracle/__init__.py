@@ -70,6 +70,10 @@ def load() -> ctypes.CDLL:
         lib.oracle_cmp_results.restype = _i
         lib.oracle_im2col.argtypes = [_f32p, _i, _i, _i, _i, _i, _i, _f32p]
         lib.oracle_im2col.restype = None
+        lib.oracle_saxpy_cpu.argtypes = [_i, _f, _f32p, _i, _f32p, _i]
+        lib.oracle_saxpy_cpu.restype = None
+        lib.oracle_sgemv_cpu.argtypes = [_c, _i, _i, _f, _f32p, _i, _f32p, _i, _f, _f32p, _i]
+        lib.oracle_sgemv_cpu.restype = None
         _lib = lib
     return _lib
 
@@ -85,6 +89,10 @@ def load_ref(fast: bool) -> ctypes.CDLL:
         getattr(lib, name).restype = None
     lib.ref_cmp_results.argtypes = [_i, _i, _f32p, _f32p, _i]
     lib.ref_cmp_results.restype = None
+    lib.saxpy_cpu.argtypes = [_i, _f, _f32p, _i, _f32p, _i]
+    lib.saxpy_cpu.restype = None
+    lib.sgemv_cpu.argtypes = [_c, _i, _i, _f, _f32p, _i, _f32p, _i, _f, _f32p, _i]
+    lib.sgemv_cpu.restype = None
     return lib
 
 

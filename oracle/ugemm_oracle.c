@@ -19,6 +19,8 @@
  *   oracle_sgemm_avx256_mt  band-parallel harness around the above (all trans)
  *   oracle_cmp_results    check_sgemm.c:56-85  stdErr/stdRef/maxErr metric
  *   oracle_im2col         sgemm_ocl1.h:81-119  im2col (one image, square kernel)
+ *   oracle_saxpy_cpu      ugemm.h:86-97        y += alpha*x with strides
+ *   oracle_sgemv_cpu      ugemm.h:129-160      column-major GEMV (x read with incy)
  *
  * Build flags matter and are fixed by oracle/Makefile: the naive and blocked
  * restatements are compiled with -ffp-contract=off (no fused multiply-add, no
@@ -231,4 +233,25 @@ void oracle_im2col(const float *im, int channels, int height, int width, int ksi
                                               : 0.f;
                     }
             }
+}
+
+/* ugemm.h:86-97 (saxpy_cpu): y[n*incy] += alpha * x[n*incx]. */
+void oracle_saxpy_cpu(int N, float alpha, const float *x, int incx, float *y, int incy)
+{
+    for (int n = 0; n < N; n++) y[n * incy] += alpha * x[n * incx];
+}
+
+/* ugemm.h:129-160 (sgemv_cpu).  Column-major A; 'N': sum over n of
+ * A[m + n*lda] * x[n*incy]; otherwise A[n + m*lda] * x[n*incy] (the
+ * reference indexes x with incy); y[m*incy] = alpha*sum + beta*y[m*incy]. */
+void oracle_sgemv_cpu(char trans, int M, int N, float alpha, const float *A, int lda,
+                      const float *x, int incx, float beta, float *y, int incy)
+{
+    (void)incx;
+    for (int m = 0; m < M; m++) {
+        float sum = 0.0f;
+        for (int n = 0; n < N; n++)
+            sum += (trans == 'N' ? A[m + n * lda] : A[n + m * lda]) * x[n * incy];
+        y[m * incy] = alpha * sum + beta * y[m * incy];
+    }
 }

@@ -132,6 +132,23 @@ def main() -> None:
         line = capture_stdout(lambda: strict.ref_cmp_results(M, N, ref, res, N))
         add(f"cmp/{i}", ref=ref, res=res, line=np.frombuffer(line.encode(), dtype=np.uint8))
 
+    # --- saxpy_cpu / sgemv_cpu (ugemm.h:86-160)
+    for i, (n, incx, incy) in enumerate([(37, 1, 1), (50, 2, 3)]):
+        x = rng.uniform(-1, 1, n * incx).astype(np.float32)
+        y = rng.uniform(-1, 1, n * incy).astype(np.float32)
+        yr = y.copy()
+        strict.saxpy_cpu(n, 0.75, x, incx, yr, incy)
+        add(f"axpy/{i}", x=x, y=y, meta=np.array([n, incx, incy], dtype=np.int64), out=yr)
+    for i, (trans, M, N, lda, inc) in enumerate([("N", 33, 21, 40, 1), ("T", 19, 45, 50, 1),
+                                                 ("N", 17, 9, 17, 2)]):
+        A = rng.uniform(-1, 1, lda * (N if trans == "N" else M)).astype(np.float32)
+        x = rng.uniform(-1, 1, N * inc).astype(np.float32)
+        y = rng.uniform(-1, 1, M * inc).astype(np.float32)
+        yr = y.copy()
+        strict.sgemv_cpu(trans.encode(), M, N, 1.5, A, lda, x, inc, 0.5, yr, inc)
+        add(f"gemv/{i}", A=A, x=x, y=y, flags=np.frombuffer(trans.encode(), dtype=np.uint8),
+            meta=np.array([M, N, lda, inc], dtype=np.int64), out=yr)
+
     # --- known-answer test, sgemm_test.c:186-200 (RNN 3x3x2)
     A = np.array([[1, 2], [3, 4], [5, 6]], dtype=np.float32)
     B = np.array([[1, 2, 3], [4, 5, 6]], dtype=np.float32)

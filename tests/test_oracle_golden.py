@@ -130,3 +130,19 @@ def test_im2col_matches_direct_convolution():
                 patch = padded[:, i * stride:i * stride + k, j * stride:j * stride + k]
                 ref[:, i, j] = np.tensordot(wt, patch, axes=([1, 2, 3], [0, 1, 2]))
         np.testing.assert_allclose(got, ref.reshape(5, -1), rtol=1e-12, atol=1e-12)
+
+
+def test_saxpy_and_sgemv_restatements_bit_exact(golden):
+    lib = oracle.load()
+    for name in [c for c in golden["cases"] if str(c).startswith("axpy/")]:
+        g = lambda k: golden[f"{name}/{k}"]  # noqa: E731
+        n, incx, incy = (int(v) for v in g("meta"))
+        y = g("y").copy()
+        lib.oracle_saxpy_cpu(n, 0.75, g("x"), incx, y, incy)
+        assert np.array_equal(y, g("out")), name
+    for name in [c for c in golden["cases"] if str(c).startswith("gemv/")]:
+        g = lambda k: golden[f"{name}/{k}"]  # noqa: E731
+        M, N, lda, inc = (int(v) for v in g("meta"))
+        y = g("y").copy()
+        lib.oracle_sgemv_cpu(bytes(g("flags")), M, N, 1.5, g("A"), lda, g("x"), inc, 0.5, y, inc)
+        assert np.array_equal(y, g("out")), name

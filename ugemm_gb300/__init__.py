@@ -492,3 +492,31 @@ def _torch_view(addr: int, shape, torch):
     h.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (addr, False),
                                   "version": 3, "strides": None}
     return torch.as_tensor(h, device="cuda")
+
+
+# --------------------------------------------------------------------------
+# SAXPY / SGEMV (ugemm.h:86-160) on device pointers
+# --------------------------------------------------------------------------
+def _blas2_sigs(lib):
+    if getattr(lib, "_blas2_ready", False):
+        return
+    lib.ugemm_saxpy.argtypes = [_i, _f, _p, _i, _p, _i, _p]
+    lib.ugemm_saxpy.restype = _i
+    lib.ugemm_sgemv.argtypes = [_c, _i, _i, _f, _p, _i, _p, _i, _f, _p, _i, _p]
+    lib.ugemm_sgemv.restype = _i
+    lib._blas2_ready = True
+
+
+def saxpy(N, alpha, x, incx, y, incy, stream=None):
+    lib = load()
+    _blas2_sigs(lib)
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_saxpy(N, alpha, ptr(x), incx, ptr(y), incy, _stream_ptr(stream)))
+
+
+def sgemv(trans, M, N, alpha, A, lda, x, incx, beta, y, incy, stream=None):
+    lib = load()
+    _blas2_sigs(lib)
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_sgemv(trans.encode(), M, N, alpha, ptr(A), lda, ptr(x), incx, beta, ptr(y),
+                           incy, _stream_ptr(stream)))
