@@ -129,6 +129,18 @@ UGEMM_API int ugemm_sgemm_dev_noalloc(char major, char transa, char transb, int 
                                       int ldb, float beta, float *C, int ldc, int precision,
                                       void *stream);
 
+/* ugemm_sgemm_dev with a fused epilogue (row-major only):
+ *   C = act(alpha*op(A)*op(B) + beta*C + bias[row]),
+ * bias: M floats on the device or NULL; act: 0 none, 1 LeakyReLU with
+ * `slope` (0.1 is the reference's; 0 gives ReLU).  This moves the
+ * reference's post-GEMM loop of gl_convolution_LReLU (sgemm_gl1.h:210-217:
+ * add the channel bias, then x > 0 ? x : 0.1*x) into the GEMM epilogue; the
+ * leak is applied in FP32 (the reference multiplies by the double 0.1). */
+UGEMM_API int ugemm_sgemm_dev_ex(char major, char transa, char transb, int M, int N, int K,
+                                 float alpha, const float *A, int lda, const float *B, int ldb,
+                                 float beta, float *C, int ldc, const float *bias, int act,
+                                 float slope, int precision, void *stream);
+
 /* Scratch bytes ugemm_sgemm_dev needs for this call (0 for most SIMT calls). */
 UGEMM_API size_t ugemm_workspace_bytes(char major, char transa, char transb, int M, int N, int K,
                              int lda, int ldb, int precision);
@@ -164,6 +176,9 @@ typedef struct {
   int ldb;
   float *C;
   int ldc;
+  const float *bias; /* optional fused epilogue, as in ugemm_sgemm_dev_ex (NULL: none) */
+  int act;           /* 0 none, 1 LeakyReLU(slope) */
+  float slope;
 } ugemm_problem;
 
 /* Tile configuration of a grouped launch (chosen by ugemm_tune_grouped). */
@@ -221,11 +236,16 @@ UGEMM_API int ugemm_col2im(const float *col, int channels, int batch, int height
  *   backward dW_l = dY_l * col_l^T, dcol_l = W_l^T * dY_l (one grouped launch),
  *            dX_l = col2im(dcol_l) = dY_{l-1}
  * with X_{l+1} = Y_l.  The gradient entering the last layer is its own
- * output (loss 0.5 * ||Y_last||^2).  No reference counterpart beyond the
- * single-layer forward ocl_convolution. */
+ * output (loss 0.5 * ||Y_last||^2).  With act == 1 a layer computes
+ * Y_l = LeakyReLU(W_l * col_l + bias_l) in the GEMM epilogue
+ * (gl_convolution_LReLU, sgemm_gl1.h:192-218), and its backward first scales
+ * dY_l by the activation's slope where Y_l <= 0 and sums it into dbias_l.  No
+ * reference counterpart beyond the single-layer forward ocl_convolution. */
 typedef struct {
   int cin, cout, height, width; /* input channels/size of the layer */
   int ksize, pad, stride;       /* square kernel, equal padding and stride */
+  int act;                      /* 0: Y = W*col; 1: Y = LeakyReLU(W*col + bias, slope) */
+  float slope;                  /* leak of the activation (the reference uses 0.1) */
 } ugemm_conv_layer;
 
 typedef struct ugemm_conv_stack_s ugemm_conv_stack;
@@ -240,7 +260,9 @@ enum {
   UGEMM_CONV_DW = 4,
   UGEMM_CONV_DCOL = 5,
   UGEMM_CONV_DX = 6,
-  UGEMM_CONV_DY = 7
+  UGEMM_CONV_DY = 7,
+  UGEMM_CONV_BIAS = 8, /* cout floats, used when act == 1 (fill before running) */
+  UGEMM_CONV_DBIAS = 9 /* cout floats, written by the backward run when act == 1 */
 };
 
 /* Allocates every buffer and one grouped plan per layer and direction; with

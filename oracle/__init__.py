@@ -70,6 +70,8 @@ def load() -> ctypes.CDLL:
         lib.oracle_cmp_results.restype = _i
         lib.oracle_im2col.argtypes = [_f32p, _i, _i, _i, _i, _i, _i, _f32p]
         lib.oracle_im2col.restype = None
+        lib.oracle_bias_leaky.argtypes = [_f32p, _i, _i, _f32p]
+        lib.oracle_bias_leaky.restype = None
         lib.oracle_saxpy_cpu.argtypes = [_i, _f, _f32p, _i, _f32p, _i]
         lib.oracle_saxpy_cpu.restype = None
         lib.oracle_sgemv_cpu.argtypes = [_c, _i, _i, _f, _f32p, _i, _f32p, _i, _f, _f32p, _i]
@@ -166,3 +168,11 @@ def normwise_error(C, C64) -> float:
     C = np.asarray(C, dtype=np.float64)
     C64 = np.asarray(C64, dtype=np.float64)
     return float(np.linalg.norm(C - C64) / np.linalg.norm(C64))
+
+
+def bias_leaky(out, bias):
+    """sgemm_gl1.h:210-217 applied in place to a channels x pixels float32 array."""
+    lib = load()
+    c, n = out.shape
+    lib.oracle_bias_leaky(out, c, n, np.ascontiguousarray(bias, dtype=np.float32))
+    return out

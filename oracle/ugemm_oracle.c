@@ -21,6 +21,7 @@
  *   oracle_im2col         sgemm_ocl1.h:81-119  im2col (one image, square kernel)
  *   oracle_saxpy_cpu      ugemm.h:86-97        y += alpha*x with strides
  *   oracle_sgemv_cpu      ugemm.h:129-160      column-major GEMV (x read with incy)
+ *   oracle_bias_leaky     sgemm_gl1.h:210-217  bias + LeakyReLU(0.1) after a conv GEMM
  *
  * Build flags matter and are fixed by oracle/Makefile: the naive and blocked
  * restatements are compiled with -ffp-contract=off (no fused multiply-add, no
@@ -254,4 +255,17 @@ void oracle_sgemv_cpu(char trans, int M, int N, float alpha, const float *A, int
             sum += (trans == 'N' ? A[m + n * lda] : A[n + m * lda]) * x[n * incy];
         y[m * incy] = alpha * sum + beta * y[m * incy];
     }
+}
+
+/* sgemm_gl1.h:210-217 (the loop after the GEMM in gl_convolution_LReLU):
+ * out[c][p] += bias[c]; out = out > 0 ? out : out * 0.1, with the multiply
+ * done in double (the literal 0.1 is a double) and rounded back to float. */
+void oracle_bias_leaky(float *out, int channels, int pixels, const float *bias)
+{
+    float *p = out;
+    for (int i = 0; i < channels; i++)
+        for (int n = 0; n < pixels; n++, p++) {
+            *p += bias[i];
+            *p = *p > 0 ? (*p) : (float)((double)(*p) * 0.1);
+        }
 }

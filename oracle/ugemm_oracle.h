@@ -29,6 +29,7 @@ int oracle_sgemm_avx256_mt(int nthreads, char ta, char tb, int M, int N, int K, 
 int oracle_cmp_results(int M, int N, const float *ref, const float *res, int ld, double out[4]);
 void oracle_im2col(const float *im, int channels, int height, int width, int ksize, int pad,
                    int stride, float *col);
+void oracle_bias_leaky(float *out, int channels, int pixels, const float *bias);
 void oracle_saxpy_cpu(int N, float alpha, const float *x, int incx, float *y, int incy);
 void oracle_sgemv_cpu(char trans, int M, int N, float alpha, const float *A, int lda,
                       const float *x, int incx, float beta, float *y, int incy);

@@ -146,3 +146,12 @@ def test_saxpy_and_sgemv_restatements_bit_exact(golden):
         y = g("y").copy()
         lib.oracle_sgemv_cpu(bytes(g("flags")), M, N, 1.5, g("A"), lda, g("x"), inc, 0.5, y, inc)
         assert np.array_equal(y, g("out")), name
+
+
+def test_bias_leaky_restatement():
+    """sgemm_gl1.h:210-217 on a few values, including the double-precision leak."""
+    out = np.array([[1.0, -1.0, -3.0], [0.5, -0.25, 2.0]], dtype=np.float32)
+    oracle.bias_leaky(out, np.array([0.5, -1.0], dtype=np.float32))
+    expect = np.array([[1.5, np.float32(-0.5 * 0.1), np.float32(-2.5 * 0.1)],
+                       [np.float32(-0.5 * 0.1), np.float32(-1.25 * 0.1), 1.0]], dtype=np.float32)
+    assert np.array_equal(out, expect)

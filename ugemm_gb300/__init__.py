@@ -225,6 +225,26 @@ def sgemm_backward(ta: str, tb: str, M: int, N: int, K: int, alpha: float, A, ld
                                     lddb, _prec(precision), _stream_ptr(stream)))
 
 
+def gemm_ex(A, B, C=None, *, bias=None, act=0, slope=0.1, ta="N", tb="N", alpha=1.0, beta=0.0,
+            precision="auto", stream=None):
+    """C = act(alpha*op(A)*op(B) + beta*C + bias[row]) on row-major CUDA tensors."""
+    import torch
+    lib = load()
+    lib.ugemm_sgemm_dev_ex.argtypes = [_c, _c, _c, _i, _i, _i, _f, _p, _i, _p, _i, _f, _p, _i, _p,
+                                       _i, _f, _i, _p]
+    lib.ugemm_sgemm_dev_ex.restype = _i
+    M = A.shape[0] if ta == "N" else A.shape[1]
+    K = A.shape[1] if ta == "N" else A.shape[0]
+    N = B.shape[1] if tb == "N" else B.shape[0]
+    if C is None:
+        C = torch.empty((M, N), dtype=torch.float32, device=A.device)
+    _check(lib.ugemm_sgemm_dev_ex(b"R", ta.encode(), tb.encode(), M, N, K, alpha, A.data_ptr(),
+                                  A.stride(0), B.data_ptr(), B.stride(0), beta, C.data_ptr(),
+                                  C.stride(0), 0 if bias is None else bias.data_ptr(), act, slope,
+                                  _prec(precision), _stream_ptr(stream)))
+    return C
+
+
 def workspace_bytes(ta: str, tb: str, M: int, N: int, K: int, lda: int, ldb: int,
                     precision="auto", major: str = "R") -> int:
     return int(load().ugemm_workspace_bytes(major.encode(), ta.encode(), tb.encode(), M, N, K, lda,
@@ -265,7 +285,7 @@ class Problem(ctypes.Structure):
     """ugemm_problem: one row-major GEMM of a group (device pointers)."""
     _fields_ = [("transa", _c), ("transb", _c), ("M", _i), ("N", _i), ("K", _i),
                 ("alpha", _f), ("beta", _f), ("A", _p), ("lda", _i), ("B", _p), ("ldb", _i),
-                ("C", _p), ("ldc", _i)]
+                ("C", _p), ("ldc", _i), ("bias", _p), ("act", _i), ("slope", _f)]
 
 
 class TileConfig(ctypes.Structure):
@@ -307,9 +327,11 @@ def make_problems(specs):
     arr = (Problem * len(specs))()
     ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
     for i, s in enumerate(specs):
+        bias = s.get("bias")
         arr[i] = Problem(s["ta"].encode(), s["tb"].encode(), s["M"], s["N"], s["K"], s["alpha"],
                          s["beta"], ptr(s["A"]), s["lda"], ptr(s["B"]), s["ldb"], ptr(s["C"]),
-                         s["ldc"])
+                         s["ldc"], 0 if bias is None else ptr(bias), s.get("act", 0),
+                         s.get("slope", 0.1))
     return arr
 
 
@@ -380,13 +402,14 @@ def sgemm_grouped(problems, precision="bf16x6", stream=None):
 # im2col convolution stack
 # --------------------------------------------------------------------------
 CONV_FORWARD, CONV_BACKWARD = 1, 2
-CONV_BUFFERS = {"x": 0, "w": 1, "y": 2, "col": 3, "dw": 4, "dcol": 5, "dx": 6, "dy": 7}
+CONV_BUFFERS = {"x": 0, "w": 1, "y": 2, "col": 3, "dw": 4, "dcol": 5, "dx": 6, "dy": 7, "bias": 8,
+                "dbias": 9}
 
 
 class ConvLayer(ctypes.Structure):
     """ugemm_conv_layer."""
     _fields_ = [("cin", _i), ("cout", _i), ("height", _i), ("width", _i), ("ksize", _i),
-                ("pad", _i), ("stride", _i)]
+                ("pad", _i), ("stride", _i), ("act", _i), ("slope", _f)]
 
 
 def _conv_sigs(lib):
@@ -427,9 +450,10 @@ def col2im(col, channels, batch, height, width, ksize, pad, stride, x, stream=No
 
 
 class ConvStack:
-    """ugemm_conv_stack: layers as (cin, cout, height, width, stride[, ksize, pad])."""
+    """ugemm_conv_stack: layers as (cin, cout, height, width, stride[, ksize, pad]); with
+    leaky=slope every layer computes LeakyReLU(W*col + bias) (slope 0.1 is the reference's)."""
 
-    def __init__(self, layers, batch, precision="bf16x6", graph=True):
+    def __init__(self, layers, batch, precision="bf16x6", graph=True, leaky=None):
         lib = load()
         _conv_sigs(lib)
         self._lib = lib
@@ -438,7 +462,8 @@ class ConvStack:
             cin, cout, h, w, stride = l[:5]
             k = l[5] if len(l) > 5 else 3
             pad = l[6] if len(l) > 6 else 1
-            arr[i] = ConvLayer(cin, cout, h, w, k, pad, stride)
+            arr[i] = ConvLayer(cin, cout, h, w, k, pad, stride, 0 if leaky is None else 1,
+                               0.0 if leaky is None else float(leaky))
         self.layers = arr
         self.batch = batch
         h = _p()

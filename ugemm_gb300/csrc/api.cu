@@ -404,6 +404,26 @@ int ugemm_sgemm_dev(char major, char transa, char transb, int M, int N, int K, f
   return dev_gemm(g, precision, static_cast<cudaStream_t>(stream));
 }
 
+int ugemm_sgemm_dev_ex(char major, char transa, char transb, int M, int N, int K, float alpha,
+                       const float* A, int lda, const float* B, int ldb, float beta, float* C,
+                       int ldc, const float* bias, int act, float slope, int precision,
+                       void* stream) {
+  if ((bias || act) && major != 'R' && major != 'r')
+    return fail(UGEMM_ERR_ARG, "the fused epilogue takes row-major calls%s");
+  if (act != 0 && act != 1) return fail(UGEMM_ERR_ARG, "act must be 0 (none) or 1 (LeakyReLU)%s");
+  Gemm g;
+  ugemm_status s = make_gemm(major, transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, &g);
+  if (s != UGEMM_OK) return s;
+  if (g.M == 0 || g.N == 0) return UGEMM_OK;
+  g.epi.bias = bias;
+  g.epi.act = act;
+  g.epi.slope = slope;
+  if (g.K == 0 || g.alpha == 0.f) {
+    if (bias || act) return fail(UGEMM_ERR_UNSUPPORTED, "fused epilogue needs K > 0 and alpha != 0%s");
+  }
+  return dev_gemm(g, precision, static_cast<cudaStream_t>(stream));
+}
+
 size_t ugemm_workspace_bytes(char major, char transa, char transb, int M, int N, int K, int lda,
                              int ldb, int precision) {
   Gemm g;

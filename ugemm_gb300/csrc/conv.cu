@@ -77,6 +77,32 @@ __global__ void col2im_kernel(const float* __restrict__ col, int C, int B, int H
 
 int out_dim(int in, int k, int pad, int stride) { return (in + 2 * pad - k) / stride + 1; }
 
+// Backward of the fused epilogue Y = LeakyReLU(W*col + bias): the incoming
+// gradient dY (C x n, in place) is multiplied by the activation's slope
+// where Y <= 0, and dbias[c] = sum over the row of the masked gradient.  One
+// block per channel; fixed-order tree reduction (deterministic).
+__global__ void __launch_bounds__(256) leaky_backward_kernel(float* __restrict__ dy,
+                                                             const float* __restrict__ y,
+                                                             long long n, float slope,
+                                                             float* __restrict__ dbias) {
+  __shared__ float part[256];
+  const long long base = static_cast<long long>(blockIdx.x) * n;
+  float s = 0.f;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const float g = dy[base + i];
+    const float m = y[base + i] > 0.f ? g : g * slope;
+    dy[base + i] = m;
+    s += m;
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) dbias[blockIdx.x] = part[0];
+}
+
 int grid_for(long long n) {
   return static_cast<int>(std::min<long long>((n + 255) / 256, 148LL * 32));
 }
@@ -115,6 +141,7 @@ struct ugemm_conv_stack_s {
     long long n;          // batch * Ho * Wo (GEMM N)
     int kdim;             // cin * k * k (GEMM K)
     float *x, *col, *w, *y, *dw, *dcol, *dx;  // dy of layer l is dx of layer l+1
+    float *bias = nullptr, *dbias = nullptr;  // act == 1 only
     ugemm_grouped_plan* fwd = nullptr;
     ugemm_grouped_plan* bwd = nullptr;
   };
@@ -144,6 +171,14 @@ int run_stack(Stack* s, int what, cudaStream_t st) {
   if (what & UGEMM_CONV_BACKWARD) {
     for (int l = static_cast<int>(s->layers.size()) - 1; l >= 0; --l) {
       auto& L = s->layers[l];
+      if (L.d.act) {  // dY *= LeakyReLU'(Y); dbias = row sums
+        prof_begin(st);
+        leaky_backward_kernel<<<L.d.cout, 256, 0, st>>>(
+            (l + 1 < static_cast<int>(s->layers.size())) ? s->layers[l + 1].dx : L.y, L.y, L.n,
+            L.d.slope, L.dbias);
+        prof_end(st, kProfAux);
+        if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
+      }
       int rc = ugemm_grouped_run(L.bwd, st);
       if (rc != UGEMM_OK) return rc;
       ugemm_status r = col2im_launch(L.dcol, L.d.cin, s->batch, L.d.height, L.d.width,
@@ -205,7 +240,7 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
   for (int l = 0; l < nlayers; ++l) {
     const ugemm_conv_layer& d = layers[l];
     if (d.cin <= 0 || d.cout <= 0 || d.height <= 0 || d.width <= 0 || d.ksize <= 0 || d.pad < 0 ||
-        d.stride <= 0) {
+        d.stride <= 0 || (d.act != 0 && d.act != 1)) {
       destroy_stack(s);
       return UGEMM_ERR_ARG;
     }
@@ -235,6 +270,8 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     off.push_back(take(size_t(L.d.cout) * L.kdim));            // dw
     off.push_back(take(size_t(L.kdim) * L.n));                 // dcol
     off.push_back(take(size_t(L.d.cin) * batch * L.d.height * L.d.width));  // dx
+    off.push_back(take(size_t(L.d.cout)));                     // bias
+    off.push_back(take(size_t(L.d.cout)));                     // dbias
   }
   if (cudaMalloc(&s->arena, bytes) != cudaSuccess) { s->arena = nullptr; destroy_stack(s); return UGEMM_ERR_ALLOC; }
   cudaMemset(s->arena, 0, bytes);
@@ -243,12 +280,14 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
   for (size_t l = 0; l < s->layers.size(); ++l) {
     auto& L = s->layers[l];
     L.x = l == 0 ? at(x0) : s->layers[l - 1].y;
-    L.col = at(off[6 * l]);
-    L.w = at(off[6 * l + 1]);
-    L.y = at(off[6 * l + 2]);
-    L.dw = at(off[6 * l + 3]);
-    L.dcol = at(off[6 * l + 4]);
-    L.dx = at(off[6 * l + 5]);
+    L.col = at(off[8 * l]);
+    L.w = at(off[8 * l + 1]);
+    L.y = at(off[8 * l + 2]);
+    L.dw = at(off[8 * l + 3]);
+    L.dcol = at(off[8 * l + 4]);
+    L.dx = at(off[8 * l + 5]);
+    L.bias = at(off[8 * l + 6]);
+    L.dbias = at(off[8 * l + 7]);
   }
   for (size_t l = 0; l < s->layers.size(); ++l) {
     auto& L = s->layers[l];
@@ -259,11 +298,12 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     }
     const int M = L.d.cout, N = static_cast<int>(L.n), K = L.kdim;
     // forward: y = w * col
-    ugemm_problem f{'N', 'N', M, N, K, 1.f, 0.f, L.w, K, L.col, N, L.y, N};
+    ugemm_problem f{'N', 'N', M, N, K, 1.f, 0.f, L.w, K, L.col, N, L.y, N,
+                    L.d.act ? L.bias : nullptr, L.d.act, L.d.slope};
     // backward: dw = dy * col^T, dcol = w^T * dy
     const float* g = dy ? dy : L.y;
-    ugemm_problem b[2] = {{'N', 'T', M, K, N, 1.f, 0.f, g, N, L.col, N, L.dw, K},
-                          {'T', 'N', K, N, M, 1.f, 0.f, L.w, K, g, N, L.dcol, N}};
+    ugemm_problem b[2] = {{'N', 'T', M, K, N, 1.f, 0.f, g, N, L.col, N, L.dw, K, nullptr, 0, 0.f},
+                          {'T', 'N', K, N, M, 1.f, 0.f, L.w, K, g, N, L.dcol, N, nullptr, 0, 0.f}};
     int rc = ugemm_grouped_plan_create(1, &f, s->form, nullptr, 0, &L.fwd);
     if (rc == UGEMM_OK) rc = ugemm_grouped_plan_create(2, b, s->form, nullptr, 0, &L.bwd);
     if (rc != UGEMM_OK) { destroy_stack(s); return rc; }
@@ -306,6 +346,8 @@ UGEMM_API int ugemm_conv_stack_buffer(ugemm_conv_stack* s, int layer, int which,
     case UGEMM_CONV_DW: *ptr = L.dw; n = size_t(L.d.cout) * L.kdim; break;
     case UGEMM_CONV_DCOL: *ptr = L.dcol; n = size_t(L.kdim) * L.n; break;
     case UGEMM_CONV_DX: *ptr = L.dx; n = x_n; break;
+    case UGEMM_CONV_BIAS: *ptr = L.bias; n = L.d.cout; break;
+    case UGEMM_CONV_DBIAS: *ptr = L.dbias; n = L.d.cout; break;
     case UGEMM_CONV_DY:
       *ptr = (layer + 1 < static_cast<int>(s->layers.size())) ? s->layers[layer + 1].dx : L.y;
       n = size_t(L.d.cout) * L.n;

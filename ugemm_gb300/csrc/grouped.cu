@@ -126,6 +126,9 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
       return plan_fail(UGEMM_ERR_ARG, "leading dimension smaller than the matrix width");
     if (!q.C || (q.K > 0 && (!q.A || !q.B))) return plan_fail(UGEMM_ERR_ARG, "NULL operand");
     g[i] = Gemm{ta, tb, q.M, q.N, q.K, q.alpha, q.beta, q.A, q.lda, q.B, q.ldb, q.C, q.ldc};
+    g[i].epi.bias = q.bias;
+    g[i].epi.act = q.act;
+    g[i].epi.slope = q.slope;
   }
   // longest k first (round-robin tile order then balances better)
   std::vector<int> order(count);
@@ -218,7 +221,7 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
                                x.N, x.K, ld_a[j], ld_b[j], &maps[2 * j], &maps[2 * j + 1]);
       const int bm = p->cfg.block_n;
       SimtProblem sp{x.C, x.M, x.N, x.ldc, x.alpha, x.beta, cdiv(x.K, kBK), cdiv(x.M, bm),
-                     cdiv(x.N, bm), tiles};
+                     cdiv(x.N, bm), tiles, x.epi};
       if (x.K == 0) sp.nkt = 1;  // one zero-filled k tile keeps the pipeline uniform
       tiles += sp.tiles_m * sp.tiles_n;
       sprobs.push_back(sp);

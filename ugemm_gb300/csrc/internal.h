@@ -18,6 +18,17 @@ namespace ugemm {
 // ta == 'N': A is M x K (lda >= K);  ta == 'T': A is K x M (lda >= M).
 // tb == 'N': B is K x N (ldb >= N);  tb == 'T': B is N x K (ldb >= K).
 // beta == 0 means C is written without being read.
+// Optional fused epilogue: C = act(alpha*op(A)op(B) + beta*C + bias[row]),
+// act = LeakyReLU(slope) when `act` is non-zero (slope 0: ReLU).  This is the
+// reference's post-GEMM loop of gl_convolution_LReLU (sgemm_gl1.h:210-217),
+// which adds the per-channel bias and applies a 0.1 leak, moved into the
+// GEMM epilogue.  Plain data, shared with the kernels.
+struct Epilogue {
+  const float* bias = nullptr;
+  int act = 0;
+  float slope = 0.1f;
+};
+
 struct Gemm {
   char ta, tb;
   int M, N, K;
@@ -28,7 +39,16 @@ struct Gemm {
   int ldb;
   float* C;
   int ldc;
+  Epilogue epi{};
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float epilogue_apply(float v, const Epilogue& e, int row) {
+  if (e.bias) v += e.bias[row];
+  if (e.act) v = v > 0.f ? v : v * e.slope;
+  return v;
+}
+#endif
 
 // Device scratch handed to a launcher.  `bytes` is what is available at `ptr`.
 struct Scratch {

@@ -163,6 +163,7 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
     gb.lda = g.ta == 'N' ? g.lda : band_p;
     gb.B = dB;
     gb.C = dC[s];
+    if (gb.epi.bias) gb.epi.bias += m0;  // per-row bias follows the band
     gb.ldc = ldc_d;
     ugemm_status st;
     if (split) {

@@ -168,7 +168,8 @@ __device__ __forceinline__ void simt_consume(const float* As, const float* Bs, f
 // alpha/beta epilogue of one tile from registers; C is not read when beta == 0.
 template <int TM, int TN, bool AK, bool BKM>
 __device__ __forceinline__ void simt_store(const float (&acc)[TM][TN], float* C, int M, int N,
-                                           int ldc, float alpha, float beta, int m0, int n0) {
+                                           int ldc, float alpha, float beta, int m0, int n0,
+                                           const Epilogue& epi) {
   const int tid = threadIdx.x;
   const int ty = tid >> 4, tx = tid & 15;
   const bool vec = ((ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
@@ -184,7 +185,7 @@ __device__ __forceinline__ void simt_store(const float (&acc)[TM][TN], float* C,
         if (col < N) {
           float v = alpha * acc[i][j];
           if (beta != 0.f) v += beta * crow[col];
-          crow[col] = v;
+          crow[col] = epilogue_apply(v, epi, row);
         }
       }
     } else {
@@ -198,6 +199,8 @@ __device__ __forceinline__ void simt_store(const float (&acc)[TM][TN], float* C,
             const float4 o = *reinterpret_cast<const float4*>(crow + col);
             v.x += beta * o.x; v.y += beta * o.y; v.z += beta * o.z; v.w += beta * o.w;
           }
+          v.x = epilogue_apply(v.x, epi, row); v.y = epilogue_apply(v.y, epi, row);
+          v.z = epilogue_apply(v.z, epi, row); v.w = epilogue_apply(v.w, epi, row);
           *reinterpret_cast<float4*>(crow + col) = v;
         } else {
 #pragma unroll
@@ -205,7 +208,7 @@ __device__ __forceinline__ void simt_store(const float (&acc)[TM][TN], float* C,
             if (col + jj < N) {
               float v = alpha * acc[i][4 * g + jj];
               if (beta != 0.f) v += beta * crow[col + jj];
-              crow[col + jj] = v;
+              crow[col + jj] = epilogue_apply(v, epi, row);
             }
         }
       }
@@ -226,8 +229,8 @@ template <int TM, int TN, bool AK, bool BKM>
 __global__ void __launch_bounds__(kThreads, 1)
     simt_sgemm_kernel(const __grid_constant__ CUtensorMap tmA,
                       const __grid_constant__ CUtensorMap tmB, float* __restrict__ C, int M,
-                      int N, int K, int ldc, float alpha, float beta, int tiles_m, int tiles_n,
-                      int* err) {
+                      int N, int K, int ldc, float alpha, float beta, Epilogue epi, int tiles_m,
+                      int tiles_n, int* err) {
   using S = SimtShape<TM, TN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -270,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   float acc[TM][TN];
   uint32_t it = 0;
   if (!simt_mainloop<TM, TN, AK, BKM>(smem, full, empty, nkt, it, acc, err)) return;
-  simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0);
+  simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0, epi);
 }
 
 // Producer-less variant: 8 warps only.  With no ninth warp every thread may
@@ -282,8 +285,8 @@ template <int TM, int TN, bool AK, bool BKM>
 __global__ void __launch_bounds__(kConsumerWarps * 32, 1)
     simt_sgemm_np_kernel(const __grid_constant__ CUtensorMap tmA,
                          const __grid_constant__ CUtensorMap tmB, float* __restrict__ C, int M,
-                         int N, int K, int ldc, float alpha, float beta, int tiles_m, int tiles_n,
-                         int* err) {
+                         int N, int K, int ldc, float alpha, float beta, Epilogue epi,
+                         int tiles_m, int tiles_n, int* err) {
   using S = SimtShape<TM, TN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(kConsumerWarps * 32, 1)
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
-  simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0);
+  simt_store<TM, TN, AK, BKM>(acc, C, M, N, ldc, alpha, beta, m0, n0, epi);
 }
 
 // Persistent grouped SIMT GEMM: one CTA per SM walks the tiles of all
@@ -409,7 +412,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     locate(t, P, p, m0, n0);
     float acc[TM][TN];
     if (!simt_mainloop<TM, TN, false, false>(smem, full, empty, P.nkt, it, acc, err)) return;
-    simt_store<TM, TN, false, false>(acc, P.C, P.M, P.N, P.ldc, P.alpha, P.beta, m0, n0);
+    simt_store<TM, TN, false, false>(acc, P.C, P.M, P.N, P.ldc, P.alpha, P.beta, m0, n0, P.epi);
   }
 }
 
@@ -512,8 +515,8 @@ ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, in
   else     ok = encode_tmap_2d(&tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, B, g.N, g.K, ldb * 4ull,
                                S::BN, kBK, CU_TENSOR_MAP_SWIZZLE_NONE);
   if (!ok) return UGEMM_ERR_CUDA;
-  void (*kern)(const CUtensorMap, const CUtensorMap, float*, int, int, int, int, float, float, int,
-               int, int*);
+  void (*kern)(const CUtensorMap, const CUtensorMap, float*, int, int, int, int, float, float,
+               Epilogue, int, int, int*);
   if constexpr (NP) kern = simt_sgemm_np_kernel<TM, TN, AK, BKM>;
   else kern = simt_sgemm_kernel<TM, TN, AK, BKM>;
   const int threads = NP ? kConsumerWarps * 32 : kThreads;
@@ -527,7 +530,7 @@ ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, in
   const int tiles_m = cdiv(g.M, S::BM), tiles_n = cdiv(g.N, S::BN);
   prof_begin(st);
   kern<<<tiles_m * tiles_n, threads, S::SMEM, st>>>(ta, tb, g.C, g.M, g.N, g.K, g.ldc, g.alpha,
-                                                     g.beta, tiles_m, tiles_n, dev_err);
+                                                     g.beta, g.epi, tiles_m, tiles_n, dev_err);
   prof_end(st, kProfSimt);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }

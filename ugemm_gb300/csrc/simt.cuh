@@ -32,6 +32,7 @@ struct SimtProblem {
   int nkt;              // k tiles of kBK
   int tiles_m, tiles_n;
   int tile_start;
+  Epilogue epi;
 };
 
 // One operand of the batched FP32 pack: op(X) (rows x K) -> dst[k][r] with

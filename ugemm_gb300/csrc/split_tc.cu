@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
               float v = P.alpha * stage[rr * 33 + lane];
               if (P.beta != 0.f) v += P.beta * *cp;
-              *cp = v;
+              *cp = epilogue_apply(v, P.epi, row);
             }
           }
           __syncwarp();
@@ -326,6 +326,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const float4 o = *reinterpret_cast<const float4*>(crow + col0 + j);
               v.x += P.beta * o.x; v.y += P.beta * o.y; v.z += P.beta * o.z; v.w += P.beta * o.w;
             }
+            v.x = epilogue_apply(v.x, P.epi, row); v.y = epilogue_apply(v.y, P.epi, row);
+            v.z = epilogue_apply(v.z, P.epi, row); v.w = epilogue_apply(v.w, P.epi, row);
             *reinterpret_cast<float4*>(crow + col0 + j) = v;
           }
         } else {
@@ -334,7 +336,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (col0 + j < P.N) {
               float v = P.alpha * acc[j];
               if (P.beta != 0.f) v += P.beta * crow[col0 + j];
-              crow[col0 + j] = v;
+              crow[col0 + j] = epilogue_apply(v, P.epi, row);
             }
         }
       }
@@ -687,6 +689,7 @@ TcProblem split_problem(const Gemm& g, int block_n, int tile_start) {
   P.tiles_m = cdiv(g.M, kTcBM);
   P.tiles_n = cdiv(g.N, block_n);
   P.tile_start = tile_start;
+  P.epi = g.epi;
   return P;
 }
 

@@ -44,6 +44,7 @@ struct TcProblem {
   int nkb;              // k-blocks of kTcKB
   int tiles_m, tiles_n;
   int tile_start;       // first global tile index of this problem
+  Epilogue epi;
 };
 
 // One operand to split in the batched pre-pass.
