@@ -167,6 +167,8 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   if (!simt) {
     p->split = split_plan_for(form, g[0]);
     p->split.block_n = p->cfg.block_n;
+    p->split.epi = false;
+    for (const Gemm& x : g) p->split.epi |= x.epi.bias != nullptr || x.epi.act != 0;
     pieces = p->split.pieces;
   }
   std::vector<int> ld_a(count), ld_b(count);

@@ -95,7 +95,7 @@ __device__ __forceinline__ TileCoord tile_coord(const TcProblem& single, const T
   return tc;
 }
 
-template <int NP, int BN, bool GROUPED>
+template <int NP, int BN, bool GROUPED, bool EPI>
 __global__ void __launch_bounds__(kTcThreads, 1)
     split_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
@@ -285,7 +285,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmem_empty[buf]);
-      // alpha/beta epilogue (C not read when beta == 0)
+      // alpha/beta epilogue (C not read when beta == 0).  The bias /
+      // activation exists only in the EPI instantiation, so the plain kernel's
+      // epilogue carries no code for it.
+      const bool has_epi = EPI && (P.epi.bias != nullptr || P.epi.act != 0);
       if constexpr (S::STAGE_C) {
         // transpose each 32 x 32 block through shared memory: lane = column,
         // one 128-byte row segment per store instruction
@@ -299,13 +302,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           __syncwarp();
           const int cc = col + c32 * 32;
           if (cc < P.N) {
-            for (int rr = 0; rr < 32; ++rr) {
-              const int row = tc.m0 + q * 32 + rr;
-              if (row >= P.M) break;
-              float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
-              float v = P.alpha * stage[rr * 33 + lane];
-              if (P.beta != 0.f) v += P.beta * *cp;
-              *cp = epilogue_apply(v, P.epi, row);
+            if (has_epi) {
+              for (int rr = 0; rr < 32; ++rr) {
+                const int row = tc.m0 + q * 32 + rr;
+                if (row >= P.M) break;
+                float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
+                float v = P.alpha * stage[rr * 33 + lane];
+                if (P.beta != 0.f) v += P.beta * *cp;
+                *cp = epilogue_apply(v, P.epi, row);
+              }
+            } else {
+              for (int rr = 0; rr < 32; ++rr) {
+                const int row = tc.m0 + q * 32 + rr;
+                if (row >= P.M) break;
+                float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
+                float v = P.alpha * stage[rr * 33 + lane];
+                if (P.beta != 0.f) v += P.beta * *cp;
+                *cp = v;
+              }
             }
           }
           __syncwarp();
@@ -317,7 +331,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         float* crow = P.C + static_cast<size_t>(row) * P.ldc;
         const int col0 = tc.n0 + col_off;
         const bool vec = ((P.ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(P.C) & 15) == 0);
-        if (vec && col0 + HALF <= P.N) {
+        if (has_epi) {
+#pragma unroll
+          for (int j = 0; j < HALF; ++j)
+            if (col0 + j < P.N) {
+              float v = P.alpha * acc[j];
+              if (P.beta != 0.f) v += P.beta * crow[col0 + j];
+              crow[col0 + j] = epilogue_apply(v, P.epi, row);
+            }
+        } else if (vec && col0 + HALF <= P.N) {
 #pragma unroll
           for (int j = 0; j < HALF; j += 4) {
             float4 v = make_float4(P.alpha * acc[j], P.alpha * acc[j + 1], P.alpha * acc[j + 2],
@@ -326,8 +348,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const float4 o = *reinterpret_cast<const float4*>(crow + col0 + j);
               v.x += P.beta * o.x; v.y += P.beta * o.y; v.z += P.beta * o.z; v.w += P.beta * o.w;
             }
-            v.x = epilogue_apply(v.x, P.epi, row); v.y = epilogue_apply(v.y, P.epi, row);
-            v.z = epilogue_apply(v.z, P.epi, row); v.w = epilogue_apply(v.w, P.epi, row);
             *reinterpret_cast<float4*>(crow + col0 + j) = v;
           }
         } else {
@@ -336,7 +356,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (col0 + j < P.N) {
               float v = P.alpha * acc[j];
               if (P.beta != 0.f) v += P.beta * crow[col0 + j];
-              crow[col0 + j] = epilogue_apply(v, P.epi, row);
+              crow[col0 + j] = v;
             }
         }
       }
@@ -612,13 +632,13 @@ int sm_count() {
   return sms;
 }
 
-template <int NP, int BN, bool GROUPED>
+template <int NP, int BN, bool GROUPED, bool EPI>
 ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcProblem& single,
                            const CUtensorMap* maps, const TcProblem* probs, int nprob,
                            int total_tiles, int nprod, int chunk_kb, int max_ctas, int* dev_err,
                            cudaStream_t st) {
   using S = TcShape<NP, BN>;
-  auto kern = split_tc_kernel<NP, BN, GROUPED>;
+  auto kern = split_tc_kernel<NP, BN, GROUPED, EPI>;
   static bool attr_set = false;
   if (!attr_set) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -656,6 +676,7 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
     default: p.pieces = 3; p.products = 6; break;
   }
   p.block_n = (g.N > 128) ? 256 : 128;
+  p.epi = g.epi.bias != nullptr || g.epi.act != 0;
   return p;
 }
 
@@ -733,18 +754,20 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                const TcProblem* probs, int nprob, int total_tiles, int chunk_kb,
                                int max_ctas, int* dev_err, cudaStream_t st) {
   const bool grouped = probs != nullptr;
-#define UGEMM_SPLIT_CASE(NP, BN)                                                              \
-  if (p.pieces == NP && p.block_n == BN)                                                     \
-    return grouped ? launch_kernel<NP, BN, true>(ta, tb, single, maps, probs, nprob,         \
-                                                 total_tiles, p.products, chunk_kb, max_ctas, \
-                                                 dev_err, st)                                 \
-                   : launch_kernel<NP, BN, false>(ta, tb, single, maps, probs, nprob,        \
-                                                  total_tiles, p.products, chunk_kb,         \
-                                                  max_ctas, dev_err, st);
-  UGEMM_SPLIT_CASE(3, 256)
-  UGEMM_SPLIT_CASE(3, 128)
-  UGEMM_SPLIT_CASE(2, 256)
-  UGEMM_SPLIT_CASE(2, 128)
+#define UGEMM_SPLIT_CASE(NP, BN, GR, EPI)                                                    \
+  if (p.pieces == NP && p.block_n == BN && grouped == GR && p.epi == EPI)                   \
+    return launch_kernel<NP, BN, GR, EPI>(ta, tb, single, maps, probs, nprob, total_tiles,   \
+                                          p.products, chunk_kb, max_ctas, dev_err, st);
+#define UGEMM_SPLIT_CASES(NP, BN)    \
+  UGEMM_SPLIT_CASE(NP, BN, false, false) \
+  UGEMM_SPLIT_CASE(NP, BN, false, true)  \
+  UGEMM_SPLIT_CASE(NP, BN, true, false)  \
+  UGEMM_SPLIT_CASE(NP, BN, true, true)
+  UGEMM_SPLIT_CASES(3, 256)
+  UGEMM_SPLIT_CASES(3, 128)
+  UGEMM_SPLIT_CASES(2, 256)
+  UGEMM_SPLIT_CASES(2, 128)
+#undef UGEMM_SPLIT_CASES
 #undef UGEMM_SPLIT_CASE
   return UGEMM_ERR_ARG;
 }
