@@ -85,6 +85,64 @@ def test_grouped_edge_cases(prec):
         assert torch.equal(s["C"][:, s["N"]:], k)  # padding untouched
 
 
+@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+def test_grouped_split_k_slices_deep_problems(prec):
+    """Weight-gradient-shaped problems (small output, k in the tens of
+    thousands) beside shallow ones: the plan cuts the deep ones into k
+    slices whose partial tiles one reduce launch sums (with beta * C)."""
+    shapes = [("N", "T", 64, 200, 40000), ("T", "N", 100, 50, 30000), ("N", "N", 300, 40, 256),
+              ("N", "T", 33, 900, 64)]
+    specs, refs = make_group(shapes, seed=7, alpha=1.25, beta=0.5, pad=1)
+    c0 = [s["C"].clone() for s in specs]
+    keep = [s["C"][:, s["N"]:].clone() for s in specs]
+    plan = ug.GroupedPlan(specs, precision=prec)
+    ug.profile_enable(True)
+    try:
+        plan.run()
+        prof = ug.profile_collect()
+    finally:
+        ug.profile_enable(False)
+    plan.check()
+    assert prof["aux"][1] == 1  # the split-K reduce ran once
+    for s, ref, k in zip(specs, refs, keep):
+        got = s["C"][:, :s["N"]].double()
+        err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        # FP32 accumulation depth of a slice, not of the whole k
+        assert err < max(2e-6, 2.5e-8 * s["K"] ** 0.5), (prec, s["M"], s["N"], s["K"], err)
+        assert torch.equal(s["C"][:, s["N"]:], k)  # padding untouched
+    # replay from the same C: bit-identical (fixed slice order)
+    first = [s["C"].clone() for s in specs]
+    for s, c in zip(specs, c0):
+        s["C"].copy_(c)
+    plan.run()
+    plan.check()
+    for s, f in zip(specs, first):
+        assert torch.equal(s["C"], f)
+    plan.close()
+
+
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9"])
+def test_grouped_wide_and_narrow_problems(prec):
+    """Few rows and many columns (computed transposed by the split form) and
+    narrow right-edge tiles (MMAs as wide as the columns, in steps of 16)."""
+    shapes = [("N", "N", 17, 1000, 300), ("T", "T", 40, 700, 129), ("N", "T", 500, 24, 64),
+              ("T", "N", 130, 145, 77), ("N", "N", 1, 4000, 33), ("N", "T", 16, 16, 16)]
+    specs, refs = make_group(shapes, seed=8, alpha=0.75, beta=-1.5, pad=5)
+    keep = [s["C"][:, s["N"]:].clone() for s in specs]
+    for bn in (128, 256):
+        plan =ug.GroupedPlan(specs, precision=prec, config={"block_n": bn, "chunk_k": 256,
+                                                            "max_ctas": 0})
+        c0 = [s["C"].clone() for s in specs]
+        plan.run()
+        plan.check()
+        assert worst_error(specs, refs) < 2e-6, bn
+        for s, k in zip(specs, keep):
+            assert torch.equal(s["C"][:, s["N"]:], k)
+        for s, c in zip(specs, c0):  # beta != 0: restore C for the next tile width
+            s["C"].copy_(c)
+        plan.close()
+
+
 def test_grouped_rejects_bad_problems():
     specs, _ = make_group([("N", "N", 8, 8, 8)])
     specs[0]["lda"] = 4  # < K

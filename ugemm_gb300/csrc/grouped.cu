@@ -39,6 +39,10 @@ struct ugemm_grouped_plan_s {
   const void* probs = nullptr;
   const void* jobs = nullptr;
   int njobs = 0, prep_tiles = 0, gemm_tiles = 0;
+  int nsub = 0;                   // kernel problems (split-K slices count one each)
+  const void* reduce = nullptr;   // split-K reduce jobs
+  int nreduce = 0;
+  long long reduce_max = 0;       // largest M x N among them
   ugemm::SplitPlan split{};
   // optional graph
   cudaGraph_t graph = nullptr;
@@ -53,14 +57,51 @@ ugemm_status plan_fail(ugemm_status s, const char* msg) {
   return s;
 }
 
+// Split-K: one GEMM of a group whose k depth dwarfs the rest is cut into
+// k slices; slice s writes alpha * op(A)[:, ks] op(B)[ks, :] into its own
+// FP32 partial tile set part + s*M*N (row-major, ld N), and one reduce
+// launch forms C = sum_s part_s + beta*C (C not read when beta == 0), then
+// the optional bias / activation.  The slices are summed in a fixed order.
+struct ReduceJob {
+  const float* part;
+  float* C;
+  int M, N, ldc, slices;
+  float beta;
+  Epilogue epi;
+};
+
+__global__ void __launch_bounds__(256) splitk_reduce_kernel(const ReduceJob* __restrict__ jobs) {
+  const ReduceJob J = jobs[blockIdx.y];
+  const long long mn = static_cast<long long>(J.M) * J.N;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < mn; i += 256LL * gridDim.x) {
+    float v = 0.f;
+    for (int s = 0; s < J.slices; ++s) v += J.part[s * mn + i];
+    const int m = static_cast<int>(i / J.N), n = static_cast<int>(i % J.N);
+    float* cp = J.C + static_cast<long long>(m) * J.ldc + n;
+    if (J.beta != 0.f) v += J.beta * *cp;
+    *cp = epilogue_apply(v, J.epi, m);
+  }
+}
+
+ugemm_status reduce_launch(const ugemm_grouped_plan_s* p, cudaStream_t st) {
+  if (p->nreduce == 0) return UGEMM_OK;
+  const long long blocks = std::min<long long>((p->reduce_max + 255) / 256, 152LL * 8);
+  prof_begin(st);
+  splitk_reduce_kernel<<<dim3(static_cast<unsigned>(blocks), p->nreduce), 256, 0, st>>>(
+      static_cast<const ReduceJob*>(p->reduce));
+  prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
 ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
   ugemm_status s;
   if (p->form == UGEMM_PREC_SIMT) {
     s = pack_batched_launch(static_cast<const PackJob*>(p->jobs), p->njobs, p->prep_tiles, st);
     if (s != UGEMM_OK) return s;
     const int tile = p->cfg.block_n == 64 ? kSimt64x64 : kSimt128x128;
-    return simt_grouped_launch(tile, p->maps, static_cast<const SimtProblem*>(p->probs), p->count,
-                               p->gemm_tiles, p->cfg.max_ctas, p->dev_err, st);
+    s = simt_grouped_launch(tile, p->maps, static_cast<const SimtProblem*>(p->probs), p->nsub,
+                            p->gemm_tiles, p->cfg.max_ctas, p->dev_err, st);
+    return s == UGEMM_OK ? reduce_launch(p, st) : s;
   }
   s = split_batched_launch(p->split.pieces, static_cast<const SplitJob*>(p->jobs), p->njobs,
                            p->prep_tiles, st);
@@ -68,9 +109,17 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
-  return split_gemm_launch(p->split, dummy, dummy, single, p->maps,
-                           static_cast<const TcProblem*>(p->probs), p->count, p->gemm_tiles,
-                           std::max(1, p->cfg.chunk_k / kTcKB), p->cfg.max_ctas, p->dev_err, st);
+  s = split_gemm_launch(p->split, dummy, dummy, single, p->maps,
+                        static_cast<const TcProblem*>(p->probs), p->nsub, p->gemm_tiles,
+                        std::max(1, p->cfg.chunk_k / kTcKB), p->cfg.max_ctas, p->dev_err, st);
+  return s == UGEMM_OK ? reduce_launch(p, st) : s;
+}
+
+// Padded tile area of an R x C output in 128 x bn tiles whose right-edge
+// tile is only as wide as its columns rounded to 16 (the split kernel's
+// narrow-N MMAs).
+double padded_area(int rows, int cols, int bn) {
+  return double(align_up(rows, 128)) * ((cols / bn) * bn + align_up(cols % bn, 16));
 }
 
 void free_plan(ugemm_grouped_plan_s* p) {
@@ -157,21 +206,72 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
     p->cfg.block_n = 128;
   }
   cudaGetDevice(&p->device);
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
   for (const Gemm& x : g) p->flops += 2.0 * x.M * x.N * x.K;
 
   const bool simt = form == UGEMM_PREC_SIMT;
-  // scratch slots
-  std::vector<size_t> a_off(count), b_off(count);
-  size_t scratch = 0;
+  const int bn = p->cfg.block_n;
   int pieces = 3;
   if (!simt) {
     p->split = split_plan_for(form, g[0]);
-    p->split.block_n = p->cfg.block_n;
-    p->split.epi = false;
-    for (const Gemm& x : g) p->split.epi |= x.epi.bias != nullptr || x.epi.act != 0;
+    p->split.block_n = bn;
     pieces = p->split.pieces;
   }
+  // Kernel geometry of each problem (in k-depth order j).  The split form
+  // computes C^T = op(B)^T op(A)^T when that wastes less of its 128-row
+  // tiles (a problem with few rows and many columns); both operands are
+  // K-major pieces either way, so only the roles of the maps swap.
+  struct Geo {
+    bool swap = false;
+    int tiles = 0, nkb = 0;  // output tiles, k-blocks (32 deep)
+    int slices = 1, per = 0; // split-K slices and their length in k-blocks
+  };
+  std::vector<Geo> geo(count);
+  double work = 0;
+  for (int j = 0; j < count; ++j) {
+    const Gemm& x = g[order[j]];
+    Geo& o = geo[j];
+    if (simt) {
+      o.tiles = cdiv(x.M, bn) * cdiv(x.N, bn);
+      o.nkb = std::max(1, cdiv(x.K, kBK));
+    } else {
+      o.swap = padded_area(x.N, x.M, bn) < padded_area(x.M, x.N, bn);
+      const int rows = o.swap ? x.N : x.M, cols = o.swap ? x.M : x.N;
+      o.tiles = cdiv(rows, kTcBM) * cdiv(cols, bn);
+      o.nkb = split_kp(x.K) / kTcKB;
+    }
+    o.per = o.nkb;
+    work += double(o.tiles) * o.nkb;
+  }
+  // Split-K.  The persistent CTAs share the group's tile k-blocks; a problem
+  // whose tiles are each longer than half an SM's fair share (a weight
+  // gradient: small output, k = batch x pixels) would leave most SMs idle,
+  // so it is cut into slices of about that length, at least kMinSlice
+  // k-blocks, and at most 1 GiB of partial tiles.
+  constexpr int kMinSlice = 16;
+  const double fair = work / (2.0 * sms);
+  std::vector<size_t> part_off(count, 0);
+  size_t part_bytes = 0;
+  for (int j = 0; j < count; ++j) {
+    const Gemm& x = g[order[j]];
+    Geo& o = geo[j];
+    if (x.K == 0 || o.nkb < 2 * kMinSlice || o.nkb <= fair) continue;
+    const int len = std::max(kMinSlice, static_cast<int>(fair) + 1);
+    const size_t tile_bytes = size_t(x.M) * x.N * 4;
+    int sl = std::min(cdiv(o.nkb, len), 256);
+    sl = static_cast<int>(std::min<size_t>(sl, (size_t(1) << 30) / tile_bytes));
+    if (sl < 2) continue;
+    o.per = cdiv(o.nkb, sl);
+    o.slices = cdiv(o.nkb, o.per);
+    part_off[j] = part_bytes;
+    part_bytes += align_up(size_t(o.slices) * tile_bytes, 256);
+  }
+
+  // scratch: operand slots, then the split-K partial tiles
+  std::vector<size_t> a_off(count), b_off(count);
   std::vector<int> ld_a(count), ld_b(count);
+  size_t scratch = 0;
   for (int j = 0; j < count; ++j) {
     const Gemm& x = g[order[j]];
     a_off[j] = scratch;
@@ -188,6 +288,8 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
       scratch += split_operand_bytes(pieces, x.N, x.K);
     }
   }
+  const size_t part_base = scratch;
+  scratch += part_bytes;
   cudaError_t e = cudaMalloc(&p->scratch, std::max<size_t>(scratch, 256));
   // zeroed once: a K == 0 problem's slot is read as one zero k tile
   if (e == cudaSuccess) e = cudaMemset(p->scratch, 0, std::max<size_t>(scratch, 256));
@@ -199,46 +301,95 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   }
   uint8_t* base = static_cast<uint8_t*>(p->scratch);
 
-  // host tables
-  std::vector<CUtensorMap> maps(2 * count);
-  std::vector<TcProblem> tprobs;
-  std::vector<SimtProblem> sprobs;
+  // pre-pass jobs: one per operand of every problem
   std::vector<SplitJob> sjobs;
   std::vector<PackJob> pjobs;
-  int tiles = 0, prep = 0;
+  int prep = 0;
   for (int j = 0; j < count; ++j) {
     const Gemm& x = g[order[j]];
     long long a_sr, a_sk, b_sr, b_sk;
     split_operand_strides(x, &a_sr, &a_sk, &b_sr, &b_sk);
+    if (simt) {
+      const int tk = cdiv(std::max(x.K, 1), 64);
+      pjobs.push_back(PackJob{x.A, a_sr, a_sk, reinterpret_cast<float*>(base + a_off[j]), x.M,
+                              x.K, ld_a[j], prep});
+      prep += cdiv(x.M, 32) * tk;
+      pjobs.push_back(PackJob{x.B, b_sr, b_sk, reinterpret_cast<float*>(base + b_off[j]), x.N,
+                              x.K, ld_b[j], prep});
+      prep += cdiv(x.N, 32) * tk;
+    } else {
+      const int kp = split_kp(x.K);
+      const int tk = cdiv(kp, 64);
+      sjobs.push_back(SplitJob{x.A, a_sr, a_sk, reinterpret_cast<__nv_bfloat16*>(base + a_off[j]),
+                               x.M, x.K, kp, prep});
+      prep += cdiv(x.M, 32) * tk;
+      sjobs.push_back(SplitJob{x.B, b_sr, b_sk, reinterpret_cast<__nv_bfloat16*>(base + b_off[j]),
+                               x.N, x.K, kp, prep});
+      prep += cdiv(x.N, 32) * tk;
+    }
+  }
+
+  // kernel problems: every slice of every problem, longest k first
+  struct Sub { int j, kb0, nkb, slice; };
+  std::vector<Sub> subs;
+  for (int j = 0; j < count; ++j)
+    for (int sidx = 0; sidx < geo[j].slices; ++sidx) {
+      const int kb0 = sidx * geo[j].per;
+      subs.push_back(Sub{j, kb0, std::min(geo[j].per, geo[j].nkb - kb0), sidx});
+    }
+  std::stable_sort(subs.begin(), subs.end(), [](const Sub& a, const Sub& b) { return a.nkb > b.nkb; });
+
+  std::vector<CUtensorMap> maps(2 * subs.size());
+  std::vector<TcProblem> tprobs;
+  std::vector<SimtProblem> sprobs;
+  std::vector<ReduceJob> rjobs;
+  int tiles = 0;
+  bool any_epi = false;
+  for (size_t i = 0; i < subs.size(); ++i) {
+    const Sub& u = subs[i];
+    const Gemm& x = g[order[u.j]];
+    const Geo& o = geo[u.j];
+    // a slice writes alpha * (its partial product) to its partial tile set
+    const bool sliced = o.slices > 1;
+    float* target = sliced ? reinterpret_cast<float*>(base + part_base + part_off[u.j]) +
+                                 size_t(u.slice) * x.M * x.N
+                           : x.C;
+    const int ldt = sliced ? x.N : x.ldc;
+    const float beta = sliced ? 0.f : x.beta;
+    const Epilogue epi = sliced ? Epilogue{} : x.epi;
+    any_epi |= epi.bias != nullptr || epi.act != 0;
     bool ok;
     if (simt) {
-      float* da = reinterpret_cast<float*>(base + a_off[j]);
-      float* db = reinterpret_cast<float*>(base + b_off[j]);
-      const int tk = cdiv(std::max(x.K, 1), 64);
-      pjobs.push_back(PackJob{x.A, a_sr, a_sk, da, x.M, x.K, ld_a[j], prep});
-      prep += cdiv(x.M, 32) * tk;
-      pjobs.push_back(PackJob{x.B, b_sr, b_sk, db, x.N, x.K, ld_b[j], prep});
-      prep += cdiv(x.N, 32) * tk;
-      ok = simt_encode_grouped(p->cfg.block_n == 64 ? kSimt64x64 : kSimt128x128, da, x.M, db,
-                               x.N, x.K, ld_a[j], ld_b[j], &maps[2 * j], &maps[2 * j + 1]);
-      const int bm = p->cfg.block_n;
-      SimtProblem sp{x.C, x.M, x.N, x.ldc, x.alpha, x.beta, cdiv(x.K, kBK), cdiv(x.M, bm),
-                     cdiv(x.N, bm), tiles, x.epi};
-      if (x.K == 0) sp.nkt = 1;  // one zero-filled k tile keeps the pipeline uniform
+      const float* da = reinterpret_cast<const float*>(base + a_off[u.j]);
+      const float* db = reinterpret_cast<const float*>(base + b_off[u.j]);
+      ok = simt_encode_grouped(bn == 64 ? kSimt64x64 : kSimt128x128, da, x.M, db, x.N, x.K,
+                               ld_a[u.j], ld_b[u.j], &maps[2 * i], &maps[2 * i + 1]);
+      SimtProblem sp{target, x.M, x.N, ldt, x.alpha, beta, u.nkb, cdiv(x.M, bn), cdiv(x.N, bn),
+                     tiles, epi};
+      sp.kt0 = u.kb0;
       tiles += sp.tiles_m * sp.tiles_n;
       sprobs.push_back(sp);
     } else {
-      auto* da = reinterpret_cast<__nv_bfloat16*>(base + a_off[j]);
-      auto* db = reinterpret_cast<__nv_bfloat16*>(base + b_off[j]);
-      const int kp = split_kp(x.K);
-      const int tk = cdiv(kp, 64);
-      sjobs.push_back(SplitJob{x.A, a_sr, a_sk, da, x.M, x.K, kp, prep});
-      prep += cdiv(x.M, 32) * tk;
-      sjobs.push_back(SplitJob{x.B, b_sr, b_sk, db, x.N, x.K, kp, prep});
-      prep += cdiv(x.N, 32) * tk;
-      ok = split_encode_maps(pieces, p->cfg.block_n, da, x.M, db, x.N, x.K, &maps[2 * j],
-                             &maps[2 * j + 1]);
-      TcProblem tp = split_problem(x, p->cfg.block_n, tiles);
+      const void* da = base + a_off[u.j];
+      const void* db = base + b_off[u.j];
+      ok = o.swap ? split_encode_maps(pieces, bn, db, x.N, da, x.M, x.K, &maps[2 * i],
+                                      &maps[2 * i + 1])
+                  : split_encode_maps(pieces, bn, da, x.M, db, x.N, x.K, &maps[2 * i],
+                                      &maps[2 * i + 1]);
+      TcProblem tp{};
+      tp.C = target;
+      tp.M = o.swap ? x.N : x.M;
+      tp.N = o.swap ? x.M : x.N;
+      tp.ldc = ldt;
+      tp.alpha = x.alpha;
+      tp.beta = beta;
+      tp.nkb = u.nkb;
+      tp.tiles_m = cdiv(tp.M, kTcBM);
+      tp.tiles_n = cdiv(tp.N, bn);
+      tp.tile_start = tiles;
+      tp.kb0 = u.kb0;
+      tp.swap = o.swap ? 1 : 0;
+      tp.epi = epi;
       tiles += tp.tiles_m * tp.tiles_n;
       tprobs.push_back(tp);
     }
@@ -246,23 +397,33 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
       free_plan(p);
       return plan_fail(UGEMM_ERR_CUDA, "tensor map encoding failed");
     }
+    if (sliced && u.slice == 0) {
+      rjobs.push_back(ReduceJob{target, x.C, x.M, x.N, x.ldc, o.slices, x.beta, x.epi});
+      p->reduce_max = std::max(p->reduce_max, static_cast<long long>(x.M) * x.N);
+    }
   }
+  if (!simt) p->split.epi = any_epi;
   p->gemm_tiles = tiles;
   p->prep_tiles = prep;
   p->njobs = 2 * count;
+  p->nsub = static_cast<int>(subs.size());
+  p->nreduce = static_cast<int>(rjobs.size());
 
-  // one device table: maps (64-byte aligned) | problems | jobs
+  // one device table: maps (64-byte aligned) | problems | jobs | reduce jobs
   const size_t maps_bytes = maps.size() * sizeof(CUtensorMap);
   const size_t prob_bytes = simt ? sprobs.size() * sizeof(SimtProblem) : tprobs.size() * sizeof(TcProblem);
   const size_t job_bytes = simt ? pjobs.size() * sizeof(PackJob) : sjobs.size() * sizeof(SplitJob);
+  const size_t red_bytes = rjobs.size() * sizeof(ReduceJob);
   const size_t off_p = align_up(maps_bytes, 256), off_j = off_p + align_up(prob_bytes, 256);
-  const size_t total = off_j + align_up(job_bytes, 256);
+  const size_t off_r = off_j + align_up(job_bytes, 256);
+  const size_t total = off_r + align_up(std::max<size_t>(red_bytes, 1), 256);
   std::vector<uint8_t> host(total, 0);
   std::memcpy(host.data(), maps.data(), maps_bytes);
   std::memcpy(host.data() + off_p, simt ? static_cast<const void*>(sprobs.data()) : tprobs.data(),
               prob_bytes);
   std::memcpy(host.data() + off_j, simt ? static_cast<const void*>(pjobs.data()) : sjobs.data(),
               job_bytes);
+  if (red_bytes) std::memcpy(host.data() + off_r, rjobs.data(), red_bytes);
   e = cudaMalloc(&p->table, total);
   if (e == cudaSuccess) e = cudaMemcpy(p->table, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -273,6 +434,7 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   p->maps = reinterpret_cast<const CUtensorMap*>(tb);
   p->probs = tb + off_p;
   p->jobs = tb + off_j;
+  p->reduce = tb + off_r;
 
   if (flags & UGEMM_PLAN_GRAPH) {
     cudaStream_t cs;

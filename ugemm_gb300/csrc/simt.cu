@@ -398,8 +398,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
           uint8_t* sa = smem + s * S::STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_2d(sa, ma, &full[s], m0, kt * kBK);
-          tma_load_2d(sa + S::A_BYTES, mb, &full[s], n0, kt * kBK);
+          tma_load_2d(sa, ma, &full[s], m0, (P.kt0 + kt) * kBK);
+          tma_load_2d(sa + S::A_BYTES, mb, &full[s], n0, (P.kt0 + kt) * kBK);
         }
       }
     }

@@ -33,6 +33,7 @@ struct SimtProblem {
   int tiles_m, tiles_n;
   int tile_start;
   Epilogue epi;
+  int kt0 = 0;          // first k tile (a split-K slice of a grouped plan)
 };
 
 // One operand of the batched FP32 pack: op(X) (rows x K) -> dst[k][r] with

@@ -155,14 +155,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           fence_tensormap(ma);
           fence_tensormap(mb);
         }
+        const int kb0 = GROUPED ? P.kb0 : 0;  // first k-block of a split-K slice
         for (int kb = 0; kb < P.nkb; ++kb, ++it) {
           const int s = it % S::STAGES;
           const uint32_t ph = (it / S::STAGES) & 1;
           if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
           uint8_t* sa = smem + s * S::STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_3d(sa, ma, &full[s], kb * kTcKB, tc.m0, 0);
-          tma_load_3d(sa + S::A_BYTES, mb, &full[s], kb * kTcKB, tc.n0, 0);
+          tma_load_3d(sa, ma, &full[s], (kb0 + kb) * kTcKB, tc.m0, 0);
+          tma_load_3d(sa + S::A_BYTES, mb, &full[s], (kb0 + kb) * kTcKB, tc.n0, 0);
         }
       }
       if (!ok) {  // let copies still in flight land before the CTA exits
@@ -173,14 +174,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc = umma_idesc(1, 1, kTcBM, BN);
+      constexpr uint32_t idesc_full = umma_idesc(1, 1, kTcBM, BN);
       const uint32_t base = smem_u32(smem);
       uint32_t it = 0, ntile = 0;
       uint32_t nbound[NB] = {};
       bool ok = true;
       for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
         TcProblem P;
-        tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+        // a group's narrow problems and right-edge tiles multiply only the
+        // columns that exist (UMMA N in steps of 16)
+        uint32_t idesc = idesc_full;
+        if constexpr (GROUPED) {
+          const int n_rem = P.N - tc.n0;
+          if (n_rem < BN) idesc = umma_idesc(1, 1, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
+        }
         const uint32_t buf = ntile % NB, use = ntile / NB;
         const uint32_t t_main = tmem + buf * 2 * BN, t_corr = t_main + BN;
         // the epilogue must have read this buffer's previous tile
@@ -246,6 +254,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
       for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
       const int nchunks = (P.nkb + chunk_kb - 1) / chunk_kb;
+      // columns of this warp's half that hold results (grouped: narrow tiles)
+      const int n_live = GROUPED ? P.N - tc.n0 - col_off : HALF;
       for (int c = 0; c + 1 < nchunks; ++c) {
         if (!__all_sync(0xffffffffu,
                         mbar_wait(&main_full[buf], nbound[buf] & 1, err, kDevTimeoutAccum))) {
@@ -256,6 +266,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         tc_fence_after();
 #pragma unroll
         for (int c32 = 0; c32 < HALF / 32; ++c32) {
+          if (GROUPED && c32 * 32 >= n_live) break;
           uint32_t r[32];
           tmem_ld_32x32b_x32(t_buf + c32 * 32, r);
           tmem_ld_wait();
@@ -275,6 +286,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int part = 0; part < 2; ++part) {
 #pragma unroll
         for (int c32 = 0; c32 < HALF / 32; ++c32) {
+          if (GROUPED && c32 * 32 >= n_live) break;
           uint32_t r[32];
           tmem_ld_32x32b_x32(t_buf + part * BN + c32 * 32, r);
           tmem_ld_wait();
@@ -289,6 +301,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // activation exists only in the EPI instantiation, so the plain kernel's
       // epilogue carries no code for it.
       const bool has_epi = EPI && (P.epi.bias != nullptr || P.epi.act != 0);
+      if (GROUPED && P.swap) {
+        // transposed problem: this lane's kernel row is a C column, so for a
+        // fixed register the warp writes 32 consecutive floats of one C row
+        const int r = tc.m0 + q * 32 + lane;
+        if (r < P.M) {
+#pragma unroll
+          for (int j = 0; j < HALF; ++j) {
+            const int c = tc.n0 + col_off + j;
+            if (c < P.N) {
+              float* cp = P.C + static_cast<size_t>(c) * P.ldc + r;
+              float v = P.alpha * acc[j];
+              if (P.beta != 0.f) v += P.beta * *cp;
+              if (has_epi) v = epilogue_apply(v, P.epi, c);
+              *cp = v;
+            }
+          }
+        }
+        continue;
+      }
       if constexpr (S::STAGE_C) {
         // transpose each 32 x 32 block through shared memory: lane = column,
         // one 128-byte row segment per store instruction

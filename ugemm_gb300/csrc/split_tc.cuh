@@ -37,6 +37,12 @@ struct TcShape {
 };
 
 // One GEMM as the persistent kernel sees it (device-resident for groups).
+// M and N are the kernel's rows (operand "a" of the maps) and columns
+// (operand "b").  Grouped plans may also set
+//   kb0  > 0: the problem is one k slice [kb0, kb0 + nkb) of a split-K GEMM;
+//   swap = 1: the kernel computes C^T = op(B)^T op(A)^T, so kernel row r and
+//             column c are C's element (c, r), stored at C[c * ldc + r], and
+//             a bias is indexed by the kernel column.
 struct TcProblem {
   float* C;
   int M, N, ldc;
@@ -44,6 +50,8 @@ struct TcProblem {
   int nkb;              // k-blocks of kTcKB
   int tiles_m, tiles_n;
   int tile_start;       // first global tile index of this problem
+  int kb0 = 0;
+  int swap = 0;
   Epilogue epi;
 };
 
