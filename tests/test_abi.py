@@ -82,8 +82,11 @@ def test_compat_requires_init(lib):
 
 def test_workspace_query_is_host_only(lib):
     # split-precision form: 3 bf16 pieces of A (M x Kp) and B (N x Kp)
-    n = ug.workspace_bytes("N", "N", 1024, 1024, 1024, 1024, 1024, "bf16x6")
-    assert n == 2 * 3 * 1024 * 1024 * 2
+    n = ug.workspace_bytes("N", "N", 4096, 4096, 1024, 1024, 4096, "bf16x6")
+    assert n == 2 * 3 * 4096 * 1024 * 2
+    # a deep k under a small output runs as split-K slices: partial tiles too
+    pieces = 3 * (64 + 200) * 40000 * 2
+    assert ug.workspace_bytes("N", "N", 64, 200, 40000, 40000, 200, "bf16x6") > pieces + 2 * 64 * 200 * 4
     assert ug.workspace_bytes("N", "N", 1024, 1024, 1024, 1024, 1024, "simt") == 0
     # unaligned lda forces a packed copy in the SIMT form
     assert ug.workspace_bytes("N", "N", 64, 64, 63, 63, 64, "simt") > 0

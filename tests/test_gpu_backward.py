@@ -129,3 +129,18 @@ def test_backward_config3_fd_and_cpu_gradient(shape, prec):
                                     np.zeros((K, cols), dtype=np.float32))
     got_db = dB[:, :cols].cpu().numpy()
     assert np.abs(got_db - cpu_db).max() / np.abs(cpu_db).max() < 1e-5
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "T")])
+def test_backward_with_deep_narrow_gradient(ta, tb):
+    """dA of a wide, short problem is a small output with a deep k: the split
+    form runs dA as k slices beside dB, in one launch plus one reduce."""
+    M, N, K = 200, 20000, 96
+    alpha, beta_acc = 0.75, 0.5
+    A, B, W, dA0, dB0, dA, dB = run_backward(ta, tb, M, N, K, alpha, "bf16x6", 5, beta_acc)
+    A64, B64, W64 = A.double(), B.double(), W.double()
+    refA = op(alpha * (W64 @ op(B64, tb).T), ta) + beta_acc * dA0.double()
+    refB = op(alpha * (op(A64, ta).T @ W64), tb) + beta_acc * dB0.double()
+    for got, ref in ((dA, refA), (dB, refB)):
+        err = float(torch.linalg.norm(got.double() - ref) / torch.linalg.norm(ref))
+        assert err < 2e-6, (ta, tb, err)

@@ -225,3 +225,35 @@ def test_zero_k_and_zero_alpha_scale_c():
     np.testing.assert_array_equal(out, (C * np.float32(0.5)).astype(np.float32))
     out = run("N", "N", 33, 44, 5, 0.0, A, B, 0.0, C, "bf16x6")
     assert not out.any()
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+@pytest.mark.parametrize("beta", [0.5, 0.0])
+def test_deep_narrow_gemm_runs_split_k(ta, tb, beta):
+    """A small output with a deep k (a weight-gradient shape) has fewer tiles
+    than the GPU has SMs: the split form cuts k into slices whose partial
+    tiles one reduce launch sums; beta == 0 still never reads C."""
+    M, N, K = 64, 200, 40000
+    g = torch.Generator(device="cuda").manual_seed(11)
+    A = torch.rand(oracle.op_shape(ta, M, K), device="cuda", generator=g) * 2 - 1
+    B = torch.rand(oracle.op_shape(tb, K, N), device="cuda", generator=g) * 2 - 1
+    C0 = torch.rand((M, N + 3), device="cuda", generator=g) * 2 - 1
+    if beta == 0.0:
+        C0[:, :N] = float("nan")
+    C = C0.clone()
+    ug.profile_enable(True)
+    try:
+        ug.sgemm_dev(ta, tb, M, N, K, 1.5, A, A.shape[1], B, B.shape[1], beta, C, N + 3,
+                     precision="bf16x6")
+        prof = ug.profile_collect()
+    finally:
+        ug.profile_enable(False)
+    assert prof["aux"][1] == 1  # the split-K reduce
+    a64 = A.double() if ta == "N" else A.double().T
+    b64 = B.double() if tb == "N" else B.double().T
+    ref = 1.5 * (a64 @ b64)
+    if beta != 0.0:
+        ref = ref + beta * C0[:, :N].double()
+    err = float(torch.linalg.norm(C[:, :N].double() - ref) / torch.linalg.norm(ref))
+    assert err < 2e-6, err
+    assert torch.equal(C[:, N:], C0[:, N:])

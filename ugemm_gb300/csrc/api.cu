@@ -151,10 +151,17 @@ int resolve_form(int precision, const Gemm& g) {
   return UGEMM_PREC_SIMT;
 }
 
+bool is_split_form(int form) {
+  return form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9 || form == UGEMM_PREC_BF16X3;
+}
+
 size_t scratch_for(const Gemm& g, int form) {
   if (g.M == 0 || g.N == 0 || g.K == 0 || g.alpha == 0.f) return 0;
   if (form == UGEMM_PREC_SIMT) return simt_scratch_bytes(g);
-  return split_scratch_bytes(g, split_plan_for(form, g));
+  const SplitPlan p = split_plan_for(form, g);
+  // an under-filled GEMM with deep k runs as split-K slices (multi.cu)
+  if (multi_wanted(g, p)) return multi_scratch_bytes(&g, 1, p);
+  return split_scratch_bytes(g, p);
 }
 
 // Launch one GEMM on `st` using `ws` as scratch.
@@ -162,10 +169,15 @@ ugemm_status launch(const Gemm& g, int form, Scratch ws, int* dev_err, cudaStrea
   if (g.M == 0 || g.N == 0) return UGEMM_OK;
   if (g.K == 0 || g.alpha == 0.f) return scale_c_launch(g, st);
   ugemm_status s;
-  if (form == UGEMM_PREC_SIMT) s = simt_launch(g, simt_pick_tile(g), ws, dev_err, st);
-  else if (form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9 || form == UGEMM_PREC_BF16X3)
-    s = split_launch(g, split_plan_for(form, g), ws, dev_err, st);
-  else return fail(UGEMM_ERR_ARG, "unknown precision%s");
+  if (form == UGEMM_PREC_SIMT) {
+    s = simt_launch(g, simt_pick_tile(g), ws, dev_err, st);
+  } else if (is_split_form(form)) {
+    const SplitPlan p = split_plan_for(form, g);
+    s = multi_wanted(g, p) ? multi_launch(&g, 1, p, ws, dev_err, st)
+                           : split_launch(g, p, ws, dev_err, st);
+  } else {
+    return fail(UGEMM_ERR_ARG, "unknown precision%s");
+  }
   if (s == UGEMM_ERR_CUDA) {
     cudaError_t e = cudaGetLastError();
     return cuda_fail(e, "kernel launch");
@@ -453,6 +465,46 @@ int ugemm_sgemm_backward(char transa, char transb, int M, int N, int K, float al
   if (!dC && (dA || dB)) return fail(UGEMM_ERR_ARG, "dC is NULL%s");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   auto flip = [](int t) { return static_cast<char>(t == 'N' ? 'T' : 'N'); };
+  // Split forms: dA and dB as one persistent launch (multi.cu), so the tiles
+  // of both products fill the GPU together.
+  {
+    Gemm gs[2];
+    int n = 0;
+    bool together = M > 0 && N > 0 && K > 0 && alpha != 0.f && (dA || dB);
+    if (together && dA) {
+      const ugemm_status s =
+          ta == 'N' ? make_gemm('R', 'N', flip(tb), M, K, N, alpha, dC, lddc, B, ldb, beta_a, dA,
+                                ldda, &gs[n])
+                    : make_gemm('R', static_cast<char>(tb), 'T', K, M, N, alpha, B, ldb, dC, lddc,
+                                beta_a, dA, ldda, &gs[n]);
+      if (s != UGEMM_OK) return s;
+      ++n;
+    }
+    if (together && dB) {
+      const ugemm_status s =
+          tb == 'N' ? make_gemm('R', flip(ta), 'N', K, N, M, alpha, A, lda, dC, lddc, beta_b, dB,
+                                lddb, &gs[n])
+                    : make_gemm('R', 'T', static_cast<char>(ta), N, K, M, alpha, dC, lddc, A, lda,
+                                beta_b, dB, lddb, &gs[n]);
+      if (s != UGEMM_OK) return s;
+      ++n;
+    }
+    for (int i = 0; i < n; ++i) together = together && resolve_form(precision, gs[i]) == resolve_form(precision, gs[0]);
+    const int form = n > 0 ? resolve_form(precision, gs[0]) : UGEMM_PREC_SIMT;
+    if (together && is_split_form(form)) {
+      std::lock_guard<std::mutex> lock(g_mu);
+      DeviceState* d = nullptr;
+      ugemm_status s = device_state(&d);
+      if (s != UGEMM_OK) return s;
+      const SplitPlan p = split_plan_for(form, gs[0]);
+      s = ensure_workspace(*d, multi_scratch_bytes(gs, n, p), st);
+      if (s != UGEMM_OK) return s;
+      s = multi_launch(gs, n, p, Scratch{d->ws, d->ws_bytes}, d->dev_err, st);
+      if (s == UGEMM_ERR_CUDA) return cuda_fail(cudaGetLastError(), "kernel launch");
+      if (s != UGEMM_OK) return fail(s, "launch failed%s");
+      return UGEMM_OK;
+    }
+  }
   if (dA) {
     ugemm_status s;
     if (ta == 'N')  // dA[MxK] = alpha dC op(B)^T

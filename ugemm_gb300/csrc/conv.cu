@@ -19,60 +19,81 @@ namespace ugemm {
 namespace {
 
 // col[(c*k*k + ki*k + kj)][(b*Ho + i)*Wo + j] = x[c][b][i*s - p + ki][j*s - p + kj]
-// (0 outside the image).  One thread per (c, b, i, j), as the reference's
-// work-item per (c, i, j) (sgemm_ocl1.h:97-118).
-__global__ void im2col_kernel(const float* __restrict__ x, int C, int B, int H, int W, int k,
-                              int pad, int stride, int Ho, int Wo, float* __restrict__ col) {
-  const long long n_pix = static_cast<long long>(B) * Ho * Wo;
-  const long long total = n_pix * C;
-  for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < total;
-       idx += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const long long pix = idx % n_pix;
-    const int c = static_cast<int>(idx / n_pix);
-    const int j = static_cast<int>(pix % Wo);
-    const int i = static_cast<int>((pix / Wo) % Ho);
-    const int b = static_cast<int>(pix / (static_cast<long long>(Wo) * Ho));
-    const int y0 = i * stride - pad, x0 = j * stride - pad;
-    const float* src = x + (static_cast<long long>(c) * B + b) * H * W;
-    float* dst = col + static_cast<long long>(c) * k * k * n_pix + pix;
-    for (int ki = 0; ki < k; ++ki)
-      for (int kj = 0; kj < k; ++kj) {
-        const int yy = y0 + ki, xx = x0 + kj;
-        *dst = (yy >= 0 && xx >= 0 && yy < H && xx < W) ? src[yy * W + xx] : 0.f;
-        dst += n_pix;
+// (0 outside the image).  One thread per output pixel (c, b, i, j) writing
+// its k*k column entries, as the reference's work-item per (c, i, j)
+// (sgemm_ocl1.h:97-118).  Grid: y walks the image planes (c, b), x the
+// pixels of a plane, so the index arithmetic is 32-bit and per plane; the
+// common kernel sizes and strides are compile-time constants (0: runtime).
+template <int KS, int ST>
+__global__ void __launch_bounds__(256) im2col_kernel(const float* __restrict__ x, int C, int B,
+                                                     int H, int W, int k_rt, int pad, int st_rt,
+                                                     int Ho, int Wo, float* __restrict__ col) {
+  const int k = KS ? KS : k_rt, stride = ST ? ST : st_rt;
+  const int plane_px = Ho * Wo;
+  const long long n_pix = static_cast<long long>(B) * plane_px;
+  for (int plane = blockIdx.y; plane < C * B; plane += gridDim.y) {
+    const int c = plane / B, b = plane - c * B;
+    const float* src = x + static_cast<long long>(plane) * H * W;
+    float* dst0 = col + static_cast<long long>(c) * k * k * n_pix + static_cast<long long>(b) * plane_px;
+    for (int pix = blockIdx.x * 256 + threadIdx.x; pix < plane_px; pix += 256 * gridDim.x) {
+      const int i = pix / Wo, j = pix - i * Wo;
+      const int y0 = i * stride - pad, x0 = j * stride - pad;
+      float* dst = dst0 + pix;
+#pragma unroll
+      for (int ki = 0; ki < k; ++ki) {
+        const int yy = y0 + ki;
+        const bool row_in = yy >= 0 && yy < H;
+#pragma unroll
+        for (int kj = 0; kj < k; ++kj) {
+          const int xx = x0 + kj;
+          *dst = (row_in && xx >= 0 && xx < W) ? src[yy * W + xx] : 0.f;
+          dst += n_pix;
+        }
       }
+    }
   }
 }
 
-// Adjoint of im2col: dx[c][b][y][x] = sum of the col entries that read it
-// (gather form: no atomics, deterministic).
-__global__ void col2im_kernel(const float* __restrict__ col, int C, int B, int H, int W, int k,
-                              int pad, int stride, int Ho, int Wo, float* __restrict__ dx) {
-  const long long n_pix = static_cast<long long>(B) * Ho * Wo;
-  const long long total = static_cast<long long>(C) * B * H * W;
-  for (long long idx = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; idx < total;
-       idx += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const int xx = static_cast<int>(idx % W);
-    const int yy = static_cast<int>((idx / W) % H);
-    const int b = static_cast<int>((idx / (static_cast<long long>(W) * H)) % B);
-    const int c = static_cast<int>(idx / (static_cast<long long>(W) * H * B));
-    float acc = 0.f;
-    for (int ki = 0; ki < k; ++ki) {
-      const int ty = yy + pad - ki;
-      if (ty < 0 || ty % stride) continue;
-      const int i = ty / stride;
-      if (i >= Ho) continue;
-      for (int kj = 0; kj < k; ++kj) {
-        const int tx = xx + pad - kj;
-        if (tx < 0 || tx % stride) continue;
-        const int j = tx / stride;
-        if (j >= Wo) continue;
-        acc += col[(static_cast<long long>(c) * k * k + ki * k + kj) * n_pix +
-                   (static_cast<long long>(b) * Ho + i) * Wo + j];
+// Adjoint of im2col: dx[c][b][y][x] = sum of the col entries that read it,
+// taps in (ki, kj) order (gather form: no atomics, deterministic).  Same
+// plane-by-plane grid as im2col_kernel.
+template <int KS, int ST>
+__global__ void __launch_bounds__(256) col2im_kernel(const float* __restrict__ col, int C, int B,
+                                                     int H, int W, int k_rt, int pad, int st_rt,
+                                                     int Ho, int Wo, float* __restrict__ dx) {
+  const int k = KS ? KS : k_rt, stride = ST ? ST : st_rt;
+  const int plane_px = Ho * Wo, plane_in = H * W;
+  const long long n_pix = static_cast<long long>(B) * plane_px;
+  for (int plane = blockIdx.y; plane < C * B; plane += gridDim.y) {
+    const int c = plane / B, b = plane - c * B;
+    const float* src0 = col + static_cast<long long>(c) * k * k * n_pix + static_cast<long long>(b) * plane_px;
+    float* dst = dx + static_cast<long long>(plane) * plane_in;
+    for (int p = blockIdx.x * 256 + threadIdx.x; p < plane_in; p += 256 * gridDim.x) {
+      const int yy = p / W, xx = p - yy * W;
+      float acc = 0.f;
+#pragma unroll
+      for (int ki = 0; ki < k; ++ki) {
+        const int ty = yy + pad - ki;
+        if (ty < 0 || ty % stride) continue;
+        const int i = ty / stride;
+        if (i >= Ho) continue;
+#pragma unroll
+        for (int kj = 0; kj < k; ++kj) {
+          const int tx = xx + pad - kj;
+          if (tx < 0 || tx % stride) continue;
+          const int j = tx / stride;
+          if (j >= Wo) continue;
+          acc += src0[(ki * k + kj) * n_pix + i * Wo + j];
+        }
       }
+      dst[p] = acc;
     }
-    dx[idx] = acc;
   }
+}
+
+dim3 plane_grid(int planes, int plane_px) {
+  return dim3(static_cast<unsigned>(std::min(cdiv(plane_px, 256), 64)),
+              static_cast<unsigned>(std::min(planes, 65535)));
 }
 
 int out_dim(int in, int k, int pad, int stride) { return (in + 2 * pad - k) / stride + 1; }
@@ -103,19 +124,20 @@ __global__ void __launch_bounds__(256) leaky_backward_kernel(float* __restrict__
   if (threadIdx.x == 0) dbias[blockIdx.x] = part[0];
 }
 
-int grid_for(long long n) {
-  return static_cast<int>(std::min<long long>((n + 255) / 256, 148LL * 32));
-}
-
 }  // namespace
 
 ugemm_status im2col_launch(const float* x, int C, int B, int H, int W, int k, int pad, int stride,
                            float* col, cudaStream_t st) {
   const int Ho = out_dim(H, k, pad, stride), Wo = out_dim(W, k, pad, stride);
   if (Ho <= 0 || Wo <= 0) return UGEMM_ERR_ARG;
+  const dim3 grid = plane_grid(C * B, Ho * Wo);
   prof_begin(st);
-  im2col_kernel<<<grid_for(static_cast<long long>(C) * B * Ho * Wo), 256, 0, st>>>(
-      x, C, B, H, W, k, pad, stride, Ho, Wo, col);
+  if (k == 3 && stride == 1)
+    im2col_kernel<3, 1><<<grid, 256, 0, st>>>(x, C, B, H, W, k, pad, stride, Ho, Wo, col);
+  else if (k == 3 && stride == 2)
+    im2col_kernel<3, 2><<<grid, 256, 0, st>>>(x, C, B, H, W, k, pad, stride, Ho, Wo, col);
+  else
+    im2col_kernel<0, 0><<<grid, 256, 0, st>>>(x, C, B, H, W, k, pad, stride, Ho, Wo, col);
   prof_end(st, kProfAux);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
@@ -124,9 +146,14 @@ ugemm_status col2im_launch(const float* col, int C, int B, int H, int W, int k, 
                            int stride, float* dx, cudaStream_t st) {
   const int Ho = out_dim(H, k, pad, stride), Wo = out_dim(W, k, pad, stride);
   if (Ho <= 0 || Wo <= 0) return UGEMM_ERR_ARG;
+  const dim3 grid = plane_grid(C * B, H * W);
   prof_begin(st);
-  col2im_kernel<<<grid_for(static_cast<long long>(C) * B * H * W), 256, 0, st>>>(
-      col, C, B, H, W, k, pad, stride, Ho, Wo, dx);
+  if (k == 3 && stride == 1)
+    col2im_kernel<3, 1><<<grid, 256, 0, st>>>(col, C, B, H, W, k, pad, stride, Ho, Wo, dx);
+  else if (k == 3 && stride == 2)
+    col2im_kernel<3, 2><<<grid, 256, 0, st>>>(col, C, B, H, W, k, pad, stride, Ho, Wo, dx);
+  else
+    col2im_kernel<0, 0><<<grid, 256, 0, st>>>(col, C, B, H, W, k, pad, stride, Ho, Wo, dx);
   prof_end(st, kProfAux);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }

@@ -25,6 +25,38 @@
 #include "simt.cuh"
 #include "split_tc.cuh"
 
+namespace ugemm {
+namespace {
+
+// Split-K reduction: C = sum_s part_s + beta*C (C not read when beta == 0),
+// then the optional bias / activation; slices summed in a fixed order.
+__global__ void __launch_bounds__(256) splitk_reduce_kernel(const ReduceJob* __restrict__ jobs) {
+  const ReduceJob J = jobs[blockIdx.y];
+  const long long mn = static_cast<long long>(J.M) * J.N;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < mn; i += 256LL * gridDim.x) {
+    float v = 0.f;
+    for (int s = 0; s < J.slices; ++s) v += J.part[s * mn + i];
+    const int m = static_cast<int>(i / J.N), n = static_cast<int>(i % J.N);
+    float* cp = J.C + static_cast<long long>(m) * J.ldc + n;
+    if (J.beta != 0.f) v += J.beta * *cp;
+    *cp = epilogue_apply(v, J.epi, m);
+  }
+}
+
+}  // namespace
+
+ugemm_status splitk_reduce_launch(const ReduceJob* jobs, int njobs, long long max_mn,
+                                  cudaStream_t st) {
+  if (njobs <= 0) return UGEMM_OK;
+  const long long blocks = std::min<long long>((max_mn + 255) / 256, 152LL * 8);
+  prof_begin(st);
+  splitk_reduce_kernel<<<dim3(static_cast<unsigned>(blocks), njobs), 256, 0, st>>>(jobs);
+  prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+}  // namespace ugemm
+
 struct ugemm_grouped_plan_s {
   int count = 0;
   int form = UGEMM_PREC_SIMT;
@@ -57,40 +89,10 @@ ugemm_status plan_fail(ugemm_status s, const char* msg) {
   return s;
 }
 
-// Split-K: one GEMM of a group whose k depth dwarfs the rest is cut into
-// k slices; slice s writes alpha * op(A)[:, ks] op(B)[ks, :] into its own
-// FP32 partial tile set part + s*M*N (row-major, ld N), and one reduce
-// launch forms C = sum_s part_s + beta*C (C not read when beta == 0), then
-// the optional bias / activation.  The slices are summed in a fixed order.
-struct ReduceJob {
-  const float* part;
-  float* C;
-  int M, N, ldc, slices;
-  float beta;
-  Epilogue epi;
-};
-
-__global__ void __launch_bounds__(256) splitk_reduce_kernel(const ReduceJob* __restrict__ jobs) {
-  const ReduceJob J = jobs[blockIdx.y];
-  const long long mn = static_cast<long long>(J.M) * J.N;
-  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < mn; i += 256LL * gridDim.x) {
-    float v = 0.f;
-    for (int s = 0; s < J.slices; ++s) v += J.part[s * mn + i];
-    const int m = static_cast<int>(i / J.N), n = static_cast<int>(i % J.N);
-    float* cp = J.C + static_cast<long long>(m) * J.ldc + n;
-    if (J.beta != 0.f) v += J.beta * *cp;
-    *cp = epilogue_apply(v, J.epi, m);
-  }
-}
-
 ugemm_status reduce_launch(const ugemm_grouped_plan_s* p, cudaStream_t st) {
   if (p->nreduce == 0) return UGEMM_OK;
-  const long long blocks = std::min<long long>((p->reduce_max + 255) / 256, 152LL * 8);
-  prof_begin(st);
-  splitk_reduce_kernel<<<dim3(static_cast<unsigned>(blocks), p->nreduce), 256, 0, st>>>(
-      static_cast<const ReduceJob*>(p->reduce));
-  prof_end(st, kProfAux);
-  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+  return splitk_reduce_launch(static_cast<const ReduceJob*>(p->reduce), p->nreduce, p->reduce_max,
+                              st);
 }
 
 ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
@@ -389,6 +391,7 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
       tp.tile_start = tiles;
       tp.kb0 = u.kb0;
       tp.swap = o.swap ? 1 : 0;
+      tp.map = static_cast<int>(i);
       tp.epi = epi;
       tiles += tp.tiles_m * tp.tiles_n;
       tprobs.push_back(tp);

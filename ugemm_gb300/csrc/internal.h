@@ -103,6 +103,28 @@ ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st);  // C = beta*C (or 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
+// Split-K: one GEMM cut into k slices, slice s having written
+// alpha * (its partial product) to part + s*M*N (row-major, ld N).  The
+// reduce forms C = sum_s part_s + beta*C (C not read when beta == 0), then
+// the optional bias / activation, summing the slices in a fixed order.
+struct ReduceJob {
+  const float* part;
+  float* C;
+  int M, N, ldc, slices;
+  float beta;
+  Epilogue epi;
+};
+ugemm_status splitk_reduce_launch(const ReduceJob* jobs, int njobs, long long max_mn,
+                                  cudaStream_t st);
+
+// Up to kMultiMax split-precision GEMMs (and split-K slices of them) in one
+// persistent launch, scratch in the caller's workspace (multi.cu).
+constexpr int kMultiMax = 4;
+bool multi_wanted(const Gemm& g, const SplitPlan& p);  // under-filled, deep k
+size_t multi_scratch_bytes(const Gemm* gs, int n, const SplitPlan& p);
+ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& p, Scratch ws, int* dev_err,
+                          cudaStream_t st);
+
 // Grouped plans: default tile configuration and the autotuner's cache.
 ugemm_tile_config default_grouped_config(int form);
 bool tuned_config(int count, const ugemm_problem* problems, int precision, ugemm_tile_config* cfg);

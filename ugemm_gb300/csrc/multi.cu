@@ -1,0 +1,220 @@
+// multi.cu -- a few split-precision GEMMs, and split-K slices of them, in one
+// persistent launch of the grouped tensor-core kernel, with all scratch in
+// the caller's workspace: no plan, no allocation, nothing read from host
+// memory at run time (the problem table travels as a kernel parameter), so
+// it is usable inside stream capture.
+//
+// Used where one GEMM launch at a time leaves SMs idle:
+//   * ugemm_sgemm_backward: dA = alpha dC op(B)^T and dB = alpha op(A)^T dC
+//     share one launch, so the tiles of both fill the GPU together;
+//   * single GEMMs whose output has fewer tiles than the GPU has SMs and
+//     whose k is deep (a weight-gradient shape): cut into k slices whose
+//     FP32 partial tiles one reduce launch sums in a fixed order.
+// Each GEMM may also be computed transposed (C^T = op(B)^T op(A)^T) when
+// that wastes less of the 128-row tiles, as in grouped plans.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include <cstddef>
+
+#include "internal.h"
+#include "split_tc.cuh"
+
+namespace ugemm {
+namespace {
+
+constexpr int kMultiSubs = 24;  // kernel problems (slices) per launch
+constexpr int kMinSlice = 16;   // shortest slice, in 32-deep k-blocks
+
+// Everything the launch reads from device memory, filled by one small kernel
+// from its by-value parameter (at most 4 KB of parameters).
+struct MultiTable {
+  CUtensorMap maps[2 * kMultiMax];
+  TcProblem probs[kMultiSubs];
+  ReduceJob red[kMultiMax];
+};
+static_assert(sizeof(MultiTable) <= 4000, "multi table must fit the kernel parameter space");
+static_assert(sizeof(MultiTable) % 16 == 0, "multi table copies as 16-byte words");
+
+__global__ void multi_table_kernel(const __grid_constant__ MultiTable t, MultiTable* dst) {
+  const uint4* s = reinterpret_cast<const uint4*>(&t);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = threadIdx.x; i < static_cast<int>(sizeof(MultiTable) / 16); i += blockDim.x)
+    d[i] = s[i];
+  // the GEMM kernel reads the tensor maps through the tensormap proxy
+  asm volatile("fence.proxy.tensormap::generic.release.gpu;" ::: "memory");
+}
+
+double padded(int rows, int cols, int bn) {
+  return double(align_up(rows, 128)) * ((cols / bn) * bn + align_up(cols % bn, 16));
+}
+
+int sm_count() {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+struct Geo {
+  bool swap = false;
+  int tiles = 0, nkb = 0, slices = 1, per = 0;
+};
+
+// Scratch layout: per GEMM [A pieces | B pieces], then the partial tiles of
+// the sliced GEMMs, then the table.
+struct Layout {
+  Geo geo[kMultiMax];
+  int block_n = 256;
+  size_t a_off[kMultiMax], b_off[kMultiMax], part_off[kMultiMax];
+  size_t table_off = 0, total = 0;
+};
+
+Layout layout_for(const Gemm* gs, int n, const SplitPlan& p, int sms) {
+  Layout L;
+  // 256-wide tiles unless every output is narrow in its better orientation
+  int widest = 0;
+  for (int i = 0; i < n; ++i) {
+    const Gemm& g = gs[i];
+    const bool swap = padded(g.N, g.M, 256) < padded(g.M, g.N, 256);
+    widest = std::max(widest, swap ? g.M : g.N);
+  }
+  L.block_n = widest > 128 ? 256 : 128;
+  double work = 0;
+  for (int i = 0; i < n; ++i) {
+    const Gemm& g = gs[i];
+    Geo& o = L.geo[i];
+    o.swap = padded(g.N, g.M, L.block_n) < padded(g.M, g.N, L.block_n);
+    const int rows = o.swap ? g.N : g.M, cols = o.swap ? g.M : g.N;
+    o.tiles = cdiv(rows, kTcBM) * cdiv(cols, L.block_n);
+    o.nkb = split_kp(g.K) / kTcKB;
+    o.per = o.nkb;
+    work += double(o.tiles) * o.nkb;
+  }
+  // split-K: tiles no longer than about half an SM's fair share of the work
+  const double fair = work / (2.0 * sms);
+  int subs = n;
+  for (int i = 0; i < n; ++i) {
+    const Gemm& g = gs[i];
+    Geo& o = L.geo[i];
+    if (o.nkb < 2 * kMinSlice || o.nkb <= fair) continue;
+    const int len = std::max(kMinSlice, static_cast<int>(fair) + 1);
+    const size_t tile_bytes = size_t(g.M) * g.N * 4;
+    int sl = std::min(cdiv(o.nkb, len), kMultiSubs - (subs - 1));
+    sl = static_cast<int>(std::min<size_t>(sl, (size_t(512) << 20) / tile_bytes));
+    if (sl < 2) continue;
+    o.per = cdiv(o.nkb, sl);
+    o.slices = cdiv(o.nkb, o.per);
+    subs += o.slices - 1;
+  }
+  size_t off = 0;
+  for (int i = 0; i < n; ++i) {
+    L.a_off[i] = off;
+    off += split_operand_bytes(p.pieces, gs[i].M, gs[i].K);
+    L.b_off[i] = off;
+    off += split_operand_bytes(p.pieces, gs[i].N, gs[i].K);
+  }
+  for (int i = 0; i < n; ++i) {
+    L.part_off[i] = off;
+    if (L.geo[i].slices > 1) off += align_up(size_t(L.geo[i].slices) * gs[i].M * gs[i].N * 4, 256);
+  }
+  L.table_off = align_up(off, 256);
+  L.total = L.table_off + align_up(sizeof(MultiTable), 256);
+  return L;
+}
+
+}  // namespace
+
+bool multi_wanted(const Gemm& g, const SplitPlan& p) {
+  if (g.M == 0 || g.N == 0 || g.K == 0 || g.alpha == 0.f) return false;
+  const int tiles = cdiv(g.M, kTcBM) * cdiv(g.N, p.block_n);
+  return tiles < sm_count() && split_kp(g.K) / kTcKB >= 2 * kMinSlice;
+}
+
+size_t multi_scratch_bytes(const Gemm* gs, int n, const SplitPlan& p) {
+  if (n < 1 || n > kMultiMax) return 0;
+  return layout_for(gs, n, p, sm_count()).total;
+}
+
+ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch ws, int* dev_err,
+                          cudaStream_t st) {
+  if (n < 1 || n > kMultiMax) return UGEMM_ERR_ARG;
+  for (int i = 0; i < n; ++i)
+    if (gs[i].M == 0 || gs[i].N == 0 || gs[i].K == 0 || gs[i].alpha == 0.f) return UGEMM_ERR_ARG;
+  const Layout L = layout_for(gs, n, plan, sm_count());
+  if (L.total > ws.bytes) return UGEMM_ERR_ARENA_TOO_SMALL;
+  uint8_t* base = static_cast<uint8_t*>(ws.ptr);
+  SplitPlan p = plan;
+  p.block_n = L.block_n;
+  p.epi = false;
+
+  MultiTable t;
+  std::memset(&t, 0, sizeof t);
+  int nsub = 0, nred = 0, tiles = 0;
+  long long red_max = 0;
+  for (int i = 0; i < n; ++i) {
+    const Gemm& g = gs[i];
+    const Geo& o = L.geo[i];
+    void* ap = base + L.a_off[i];
+    void* bp = base + L.b_off[i];
+    long long a_sr, a_sk, b_sr, b_sk;
+    split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
+    ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st);
+    if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st);
+    if (s != UGEMM_OK) return s;
+    const bool ok = o.swap ? split_encode_maps(p.pieces, p.block_n, bp, g.N, ap, g.M, g.K,
+                                               &t.maps[2 * i], &t.maps[2 * i + 1])
+                           : split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K,
+                                               &t.maps[2 * i], &t.maps[2 * i + 1]);
+    if (!ok) return UGEMM_ERR_CUDA;
+    const bool sliced = o.slices > 1;
+    float* part = reinterpret_cast<float*>(base + L.part_off[i]);
+    for (int sidx = 0; sidx < o.slices; ++sidx) {
+      TcProblem& tp = t.probs[nsub++];
+      tp.C = sliced ? part + size_t(sidx) * g.M * g.N : g.C;
+      tp.M = o.swap ? g.N : g.M;
+      tp.N = o.swap ? g.M : g.N;
+      tp.ldc = sliced ? g.N : g.ldc;
+      tp.alpha = g.alpha;
+      tp.beta = sliced ? 0.f : g.beta;
+      tp.kb0 = sidx * o.per;
+      tp.nkb = std::min(o.per, o.nkb - tp.kb0);
+      tp.tiles_m = cdiv(tp.M, kTcBM);
+      tp.tiles_n = cdiv(tp.N, p.block_n);
+      tp.swap = o.swap ? 1 : 0;
+      tp.map = i;
+      tp.epi = sliced ? Epilogue{} : g.epi;
+      p.epi |= tp.epi.bias != nullptr || tp.epi.act != 0;
+    }
+    if (sliced) {
+      t.red[nred++] = ReduceJob{part, g.C, g.M, g.N, g.ldc, o.slices, g.beta, g.epi};
+      red_max = std::max(red_max, static_cast<long long>(g.M) * g.N);
+    }
+  }
+  // longest k first; tile offsets in that order
+  std::stable_sort(t.probs, t.probs + nsub,
+                   [](const TcProblem& a, const TcProblem& b) { return a.nkb > b.nkb; });
+  for (int j = 0; j < nsub; ++j) {
+    t.probs[j].tile_start = tiles;
+    tiles += t.probs[j].tiles_m * t.probs[j].tiles_n;
+  }
+  uint8_t* tab = base + L.table_off;
+  multi_table_kernel<<<1, 128, 0, st>>>(t, reinterpret_cast<MultiTable*>(tab));
+  if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
+  CUtensorMap dummy;
+  std::memset(&dummy, 0, sizeof dummy);
+  TcProblem single{};
+  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  ugemm_status s = split_gemm_launch(
+      p, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
+      reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), nsub, tiles, chunk, 0,
+      dev_err, st);
+  if (s != UGEMM_OK || nred == 0) return s;
+  return splitk_reduce_launch(reinterpret_cast<const ReduceJob*>(tab + offsetof(MultiTable, red)),
+                              nred, red_max, st);
+}
+
+}  // namespace ugemm

@@ -149,8 +149,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x) {
         TcProblem P;
         const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
-        const CUtensorMap* ma = GROUPED ? &maps[2 * tc.p] : &tmA;
-        const CUtensorMap* mb = GROUPED ? &maps[2 * tc.p + 1] : &tmB;
+        const CUtensorMap* ma = GROUPED ? &maps[2 * P.map] : &tmA;
+        const CUtensorMap* mb = GROUPED ? &maps[2 * P.map + 1] : &tmB;
         if (GROUPED) {
           fence_tensormap(ma);
           fence_tensormap(mb);

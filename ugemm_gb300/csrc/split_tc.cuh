@@ -52,6 +52,7 @@ struct TcProblem {
   int tile_start;       // first global tile index of this problem
   int kb0 = 0;
   int swap = 0;
+  int map = 0;          // tensor maps of this problem: maps[2 * map], maps[2 * map + 1]
   Epilogue epi;
 };
 
