@@ -209,9 +209,10 @@ def conv_forms(ug, torch, stream, steps):
     from ugemm_gb300 import workloads
     batch = 32
     layers = workloads.conv_layers(batch)
-    out = {"layers": len(layers), "batch": batch}
-    for prec in ("bf16x6", "simt"):
-        st = ug.ConvStack(layers, batch, precision=prec, graph=True)
+    out = {"layers": len(layers), "batch": batch, "im2col": "implicit (gathered in the operand pass)"}
+    for name, prec, explicit in (("bf16x6", "bf16x6", False), ("simt", "simt", False),
+                                 ("bf16x6_explicit_im2col", "bf16x6", True)):
+        st = ug.ConvStack(layers, batch, precision=prec, graph=True, im2col=explicit)
         g = torch.Generator(device="cuda").manual_seed(SEED + 5)
         cin, _, h, w, _ = layers[0]
         st.tensor(0, "x", (cin, batch * h * w)).copy_(
@@ -230,7 +231,7 @@ def conv_forms(ug, torch, stream, steps):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
-        out[prec] = {"tflops": round(st.flops() / (ms * 1e-3) / 1e12, 2), "ms": round(ms, 3),
+        out[name] = {"tflops": round(st.flops() / (ms * 1e-3) / 1e12, 2), "ms": round(ms, 3),
                      "gemm_gflop": round(st.flops() / 1e9, 1)}
         st.close()
     return out

@@ -235,7 +235,10 @@ UGEMM_API int ugemm_col2im(const float *col, int channels, int batch, int height
  *   forward  Y_l = W_l * im2col(X_l)                 (M = cout, N = B*Ho*Wo, K = cin*k*k)
  *   backward dW_l = dY_l * col_l^T, dcol_l = W_l^T * dY_l (one grouped launch),
  *            dX_l = col2im(dcol_l) = dY_{l-1}
- * with X_{l+1} = Y_l.  The gradient entering the last layer is its own
+ * with X_{l+1} = Y_l.  By default the GEMMs read col_l = im2col(X_l)
+ * implicitly: the operand pass of the forward and dW GEMMs gathers it from
+ * X_l, and no col buffer exists.  UGEMM_CONV_IM2COL materialises col_l with
+ * an im2col pass first (the reference's formulation) and keeps the buffer.  The gradient entering the last layer is its own
  * output (loss 0.5 * ||Y_last||^2).  With act == 1 a layer computes
  * Y_l = LeakyReLU(W_l * col_l + bias_l) in the GEMM epilogue
  * (gl_convolution_LReLU, sgemm_gl1.h:192-218), and its backward first scales
@@ -252,11 +255,12 @@ typedef struct ugemm_conv_stack_s ugemm_conv_stack;
 
 #define UGEMM_CONV_FORWARD 1
 #define UGEMM_CONV_BACKWARD 2
+#define UGEMM_CONV_IM2COL 2 /* create flag (with UGEMM_PLAN_GRAPH = 1): explicit im2col */
 enum {
   UGEMM_CONV_X = 0, /* layer input (fill layer 0's before a forward run) */
   UGEMM_CONV_W = 1, /* weights, cout x cin*k*k (fill before running) */
   UGEMM_CONV_Y = 2,
-  UGEMM_CONV_COL = 3,
+  UGEMM_CONV_COL = 3, /* UGEMM_CONV_IM2COL stacks only */
   UGEMM_CONV_DW = 4,
   UGEMM_CONV_DCOL = 5,
   UGEMM_CONV_DX = 6,

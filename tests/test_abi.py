@@ -5,6 +5,7 @@ import os
 import re
 import shutil
 
+import numpy as np
 import pytest
 
 import ugemm_gb300 as ug
@@ -90,3 +91,23 @@ def test_workspace_query_is_host_only(lib):
     assert ug.workspace_bytes("N", "N", 1024, 1024, 1024, 1024, 1024, "simt") == 0
     # unaligned lda forces a packed copy in the SIMT form
     assert ug.workspace_bytes("N", "N", 64, 64, 63, 63, 64, "simt") > 0
+
+
+def test_fast_division_constants_are_exact():
+    """The implicit im2col gather divides pixel and tap indices by run-time
+    constants with q = (umulhi(x, m) + x) >> s (internal.h FastDiv);
+    the constants are exact for every divisor the conv geometry can produce
+    and every index below 2^31."""
+    rng = np.random.default_rng(0)
+    divisors = list(range(1, 300)) + [3136, 784, 196, 49, 12544, 100352, 2**20 + 7, 2**30 + 3]
+    xs = np.concatenate([np.arange(0, 70000, dtype=np.uint64),
+                         rng.integers(0, 2**31, 200000, dtype=np.uint64),
+                         np.array([2**31 - 1, 2**31 - 2], dtype=np.uint64)])
+    for d in divisors:
+        s = 0
+        while (1 << s) < d:
+            s += 1
+        m = ((1 << 32) * ((1 << s) - d)) // d + 1
+        assert 0 < m <= 0xFFFFFFFF
+        q = (((xs * np.uint64(m)) >> np.uint64(32)) + xs) >> np.uint64(s)
+        assert np.array_equal(q, xs // np.uint64(d)), d

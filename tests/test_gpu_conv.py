@@ -88,18 +88,32 @@ def tol(k):
     return max(2e-6, 2.5e-8 * k ** 0.5)
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
-def test_config5_conv_stack_per_layer_fp64(prec):
+def layer_col(stack, layers, batch, l, explicit):
+    """col_l = im2col(X_l): the stack's buffer (explicit stacks) or computed
+    here by the standalone im2col (implicit stacks store none)."""
+    ci, _, h, w, s = layers[l]
+    ho, wo = (h + 2 - 3) // s + 1, (w + 2 - 3) // s + 1
+    shape = (ci * 9, batch * ho * wo)
+    if explicit:
+        return stack.tensor(l, "col", shape)
+    col = torch.empty(shape, device="cuda")
+    ug.im2col(stack.tensor(l, "x", (ci, batch * h * w)), ci, batch, h, w, 3, 1, s, col)
+    torch.cuda.synchronize()
+    return col
+
+
+@pytest.mark.parametrize("prec,explicit", [("bf16x6", False), ("simt", False), ("bf16x6", True)])
+def test_config5_conv_stack_per_layer_fp64(prec, explicit):
     batch = 32
     layers = workloads.conv_layers(batch)
     shapes = workloads.conv_gemm_shapes(batch)
-    stack = ug.ConvStack(layers, batch, precision=prec, graph=True)
+    stack = ug.ConvStack(layers, batch, precision=prec, graph=True, im2col=explicit)
     fill_stack(stack, layers, batch)
     stack.run(ug.CONV_FORWARD | ug.CONV_BACKWARD)
     torch.cuda.synchronize()
     worst = 0.0
     for l, (M, N, K) in enumerate(shapes):
-        col = stack.tensor(l, "col", (K, N)).double()
+        col = layer_col(stack, layers, batch, l, explicit).double()
         w = stack.tensor(l, "w", (M, K)).double()
         y = stack.tensor(l, "y", (M, N))
         dy = stack.tensor(l, "dy", (M, N)).double()
@@ -133,6 +147,33 @@ def test_conv_stack_graph_replay_is_deterministic():
     torch.cuda.synchronize()
     assert torch.equal(stack.tensor(0, "dw", (64, 576)), first)
     stack.close()
+
+
+@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+def test_implicit_im2col_equals_explicit(prec):
+    """Gathering col inside the operand pass reads exactly the values the
+    im2col pass would have stored: every output is bit-identical."""
+    batch = 4
+    layers = workloads.conv_layers(batch)[:7]   # includes a stride-2 layer
+    out = []
+    for explicit in (False, True):
+        stack = ug.ConvStack(layers, batch, precision=prec, graph=True, im2col=explicit)
+        fill_stack(stack, layers, batch, seed=5)
+        stack.run()
+        torch.cuda.synchronize()
+        res = []
+        for l, (ci, co, h, w, s) in enumerate(layers):
+            for name in ("y", "dw", "dcol", "dx"):
+                addr, n = stack.buffer(l, name)
+                res.append(ug._torch_view(addr, (n,), torch).clone())
+        out.append(res)
+        if not explicit:
+            with pytest.raises(ug.UgemmError) as e:
+                stack.buffer(0, "col")
+            assert e.value.status == ug.ERR_UNSUPPORTED
+        stack.close()
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
 
 
 def test_conv_stack_rejects_mismatched_layers():

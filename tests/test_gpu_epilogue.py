@@ -67,7 +67,7 @@ def test_conv_stack_with_leaky_relu_forward_and_backward():
     batch = 4
     layers = workloads.conv_layers(batch)[:5]
     shapes = workloads.conv_gemm_shapes(batch)[:5]
-    st = ug.ConvStack(layers, batch, precision="bf16x6", graph=True, leaky=0.1)
+    st = ug.ConvStack(layers, batch, precision="bf16x6", graph=True, leaky=0.1, im2col=True)
     g = torch.Generator(device="cuda").manual_seed(2)
     cin, _, h, w, _ = layers[0]
     st.tensor(0, "x", (cin, batch * h * w)).copy_(torch.rand((cin, batch * h * w), device="cuda",

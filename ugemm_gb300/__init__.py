@@ -402,6 +402,7 @@ def sgemm_grouped(problems, precision="bf16x6", stream=None):
 # im2col convolution stack
 # --------------------------------------------------------------------------
 CONV_FORWARD, CONV_BACKWARD = 1, 2
+CONV_IM2COL = 2  # create flag: materialise the im2col matrix (UGEMM_CONV_IM2COL)
 CONV_BUFFERS = {"x": 0, "w": 1, "y": 2, "col": 3, "dw": 4, "dcol": 5, "dx": 6, "dy": 7, "bias": 8,
                 "dbias": 9}
 
@@ -451,9 +452,11 @@ def col2im(col, channels, batch, height, width, ksize, pad, stride, x, stream=No
 
 class ConvStack:
     """ugemm_conv_stack: layers as (cin, cout, height, width, stride[, ksize, pad]); with
-    leaky=slope every layer computes LeakyReLU(W*col + bias) (slope 0.1 is the reference's)."""
+    leaky=slope every layer computes LeakyReLU(W*col + bias) (slope 0.1 is the reference's).
+    im2col=True materialises each layer's im2col matrix (buffer "col") before its GEMMs;
+    by default the GEMMs gather it from the layer input and there is no col buffer."""
 
-    def __init__(self, layers, batch, precision="bf16x6", graph=True, leaky=None):
+    def __init__(self, layers, batch, precision="bf16x6", graph=True, leaky=None, im2col=False):
         lib = load()
         _conv_sigs(lib)
         self._lib = lib
@@ -467,8 +470,9 @@ class ConvStack:
         self.layers = arr
         self.batch = batch
         h = _p()
-        _check(lib.ugemm_conv_stack_create(len(arr), arr, batch, _prec(precision),
-                                           PLAN_GRAPH if graph else 0, ctypes.byref(h)))
+        flags = (PLAN_GRAPH if graph else 0) | (CONV_IM2COL if im2col else 0)
+        _check(lib.ugemm_conv_stack_create(len(arr), arr, batch, _prec(precision), flags,
+                                           ctypes.byref(h)))
         self.handle = h
 
     def buffer(self, layer: int, which: str):

@@ -169,11 +169,13 @@ struct ugemm_conv_stack_s {
     int kdim;             // cin * k * k (GEMM K)
     float *x, *col, *w, *y, *dw, *dcol, *dx;  // dy of layer l is dx of layer l+1
     float *bias = nullptr, *dbias = nullptr;  // act == 1 only
+    ugemm::Im2col im;     // im2col geometry of x (the implicit operand)
     ugemm_grouped_plan* fwd = nullptr;
     ugemm_grouped_plan* bwd = nullptr;
   };
   std::vector<Layer> layers;
   int batch = 0, form = UGEMM_PREC_BF16X6;
+  bool explicit_col = false;  // UGEMM_CONV_IM2COL: materialise col per layer
   float* dy_last = nullptr;
   void* arena = nullptr;
   double flops_fwd = 0, flops_bwd = 0;
@@ -188,9 +190,11 @@ int run_stack(Stack* s, int what, cudaStream_t st) {
   using namespace ugemm;
   if (what & UGEMM_CONV_FORWARD) {
     for (auto& L : s->layers) {
-      ugemm_status r = im2col_launch(L.x, L.d.cin, s->batch, L.d.height, L.d.width, L.d.ksize,
-                                     L.d.pad, L.d.stride, L.col, st);
-      if (r != UGEMM_OK) return r;
+      if (s->explicit_col) {
+        ugemm_status r = im2col_launch(L.x, L.d.cin, s->batch, L.d.height, L.d.width, L.d.ksize,
+                                       L.d.pad, L.d.stride, L.col, st);
+        if (r != UGEMM_OK) return r;
+      }
       int rc = ugemm_grouped_run(L.fwd, st);
       if (rc != UGEMM_OK) return rc;
     }
@@ -260,6 +264,11 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
   auto* s = new Stack;
   s->batch = batch;
   s->form = precision == UGEMM_PREC_AUTO ? UGEMM_PREC_BF16X6 : precision;
+  s->explicit_col = (flags & UGEMM_CONV_IM2COL) != 0;
+  if (s->form < UGEMM_PREC_SIMT || s->form > UGEMM_PREC_BF16X3) {
+    destroy_stack(s);
+    return UGEMM_ERR_ARG;
+  }
   // shapes and arena layout
   size_t bytes = 0;
   auto take = [&](size_t n) { size_t o = bytes; bytes += align_up(n * sizeof(float), 256); return o; };
@@ -291,7 +300,7 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
   // arena: x0 | per layer {col, w, y, dw, dcol, dx} | dy_last
   const size_t x0 = take(size_t(layers[0].cin) * batch * layers[0].height * layers[0].width);
   for (auto& L : s->layers) {
-    off.push_back(take(size_t(L.kdim) * L.n));                 // col
+    off.push_back(s->explicit_col ? take(size_t(L.kdim) * L.n) : 0);  // col
     off.push_back(take(size_t(L.d.cout) * L.kdim));            // w
     off.push_back(take(size_t(L.d.cout) * L.n));               // y
     off.push_back(take(size_t(L.d.cout) * L.kdim));            // dw
@@ -307,7 +316,7 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
   for (size_t l = 0; l < s->layers.size(); ++l) {
     auto& L = s->layers[l];
     L.x = l == 0 ? at(x0) : s->layers[l - 1].y;
-    L.col = at(off[8 * l]);
+    L.col = s->explicit_col ? at(off[8 * l]) : nullptr;
     L.w = at(off[8 * l + 1]);
     L.y = at(off[8 * l + 2]);
     L.dw = at(off[8 * l + 3]);
@@ -325,14 +334,22 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     }
     const int M = L.d.cout, N = static_cast<int>(L.n), K = L.kdim;
     // forward: y = w * col
-    ugemm_problem f{'N', 'N', M, N, K, 1.f, 0.f, L.w, K, L.col, N, L.y, N,
-                    L.d.act ? L.bias : nullptr, L.d.act, L.d.slope};
+    L.im = make_im2col(L.x, L.d.cin, batch, L.d.height, L.d.width, L.d.ksize, L.d.pad,
+                       L.d.stride, L.Ho, L.Wo);
+    // col = im2col(x): the materialised buffer, or read from x by the
+    // GEMMs' operand pass
+    const Im2col* im = s->explicit_col ? nullptr : &L.im;
+    // forward: y = w * col
+    Gemm f{'N', 'N', M, N, K, 1.f, 0.f, L.w, K, L.col, N, L.y, N};
+    f.epi = Epilogue{L.d.act ? L.bias : nullptr, L.d.act, L.d.slope};
+    f.b_im2col = im;
     // backward: dw = dy * col^T, dcol = w^T * dy
     const float* g = dy ? dy : L.y;
-    ugemm_problem b[2] = {{'N', 'T', M, K, N, 1.f, 0.f, g, N, L.col, N, L.dw, K, nullptr, 0, 0.f},
-                          {'T', 'N', K, N, M, 1.f, 0.f, L.w, K, g, N, L.dcol, N, nullptr, 0, 0.f}};
-    int rc = ugemm_grouped_plan_create(1, &f, s->form, nullptr, 0, &L.fwd);
-    if (rc == UGEMM_OK) rc = ugemm_grouped_plan_create(2, b, s->form, nullptr, 0, &L.bwd);
+    Gemm b[2] = {Gemm{'N', 'T', M, K, N, 1.f, 0.f, g, N, L.col, N, L.dw, K},
+                 Gemm{'T', 'N', K, N, M, 1.f, 0.f, L.w, K, g, N, L.dcol, N}};
+    b[0].b_im2col = im;
+    ugemm_status rc = grouped_plan_build(&f, 1, s->form, nullptr, 0, &L.fwd);
+    if (rc == UGEMM_OK) rc = grouped_plan_build(b, 2, s->form, nullptr, 0, &L.bwd);
     if (rc != UGEMM_OK) { destroy_stack(s); return rc; }
     s->flops_fwd += 2.0 * M * double(N) * K;
     s->flops_bwd += 4.0 * M * double(N) * K;
@@ -369,7 +386,11 @@ UGEMM_API int ugemm_conv_stack_buffer(ugemm_conv_stack* s, int layer, int which,
     case UGEMM_CONV_X: *ptr = L.x; n = x_n; break;
     case UGEMM_CONV_W: *ptr = L.w; n = size_t(L.d.cout) * L.kdim; break;
     case UGEMM_CONV_Y: *ptr = L.y; n = size_t(L.d.cout) * L.n; break;
-    case UGEMM_CONV_COL: *ptr = L.col; n = size_t(L.kdim) * L.n; break;
+    case UGEMM_CONV_COL:
+      if (!s->explicit_col) return UGEMM_ERR_UNSUPPORTED;  // read implicitly, never stored
+      *ptr = L.col;
+      n = size_t(L.kdim) * L.n;
+      break;
     case UGEMM_CONV_DW: *ptr = L.dw; n = size_t(L.d.cout) * L.kdim; break;
     case UGEMM_CONV_DCOL: *ptr = L.dcol; n = size_t(L.kdim) * L.n; break;
     case UGEMM_CONV_DX: *ptr = L.dx; n = x_n; break;

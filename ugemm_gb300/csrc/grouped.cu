@@ -181,6 +181,21 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
     g[i].epi.act = q.act;
     g[i].epi.slope = q.slope;
   }
+  ugemm_tile_config tuned{};
+  const ugemm_tile_config* cfg = config;
+  if (!cfg && tuned_config(count, problems, form, &tuned)) cfg = &tuned;
+  return grouped_plan_build(g.data(), count, form, cfg, flags, out);
+}
+
+}  // extern "C"
+
+namespace ugemm {
+
+ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
+                                const ugemm_tile_config* config, int flags,
+                                ugemm_grouped_plan** out) {
+  *out = nullptr;
+  std::vector<Gemm> g(gs, gs + count);
   // longest k first (round-robin tile order then balances better)
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
@@ -191,7 +206,7 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   p->form = form;
   if (config) {
     p->cfg = *config;
-  } else if (!tuned_config(count, problems, form, &p->cfg)) {
+  } else {
     p->cfg = default_grouped_config(form);
     // Untuned split plans: 256-wide tiles only pay when the problems are wide
     // (measured: 128 wins on the 256-problem set with N in [32, 1024]).
@@ -311,13 +326,19 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
     const Gemm& x = g[order[j]];
     long long a_sr, a_sk, b_sr, b_sk;
     split_operand_strides(x, &a_sr, &a_sk, &b_sr, &b_sk);
+    // an implicit im2col B: rows of op(B)^T are pixels ('N') or taps ('T');
+    // the thread layout of the rows-of-taps gather is the k-contiguous one
+    const int gather = x.b_im2col ? (x.tb == 'N' ? 1 : 2) : 0;
+    if (gather) b_sk = gather == 2 ? 1 : 0;
     if (simt) {
       const int tk = cdiv(std::max(x.K, 1), 64);
       pjobs.push_back(PackJob{x.A, a_sr, a_sk, reinterpret_cast<float*>(base + a_off[j]), x.M,
                               x.K, ld_a[j], prep});
       prep += cdiv(x.M, 32) * tk;
-      pjobs.push_back(PackJob{x.B, b_sr, b_sk, reinterpret_cast<float*>(base + b_off[j]), x.N,
-                              x.K, ld_b[j], prep});
+      PackJob bj{x.B, b_sr, b_sk, reinterpret_cast<float*>(base + b_off[j]), x.N, x.K, ld_b[j],
+                 prep};
+      if (gather) { bj.gather = gather; bj.im = *x.b_im2col; }
+      pjobs.push_back(bj);
       prep += cdiv(x.N, 32) * tk;
     } else {
       const int kp = split_kp(x.K);
@@ -325,8 +346,10 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
       sjobs.push_back(SplitJob{x.A, a_sr, a_sk, reinterpret_cast<__nv_bfloat16*>(base + a_off[j]),
                                x.M, x.K, kp, prep});
       prep += cdiv(x.M, 32) * tk;
-      sjobs.push_back(SplitJob{x.B, b_sr, b_sk, reinterpret_cast<__nv_bfloat16*>(base + b_off[j]),
-                               x.N, x.K, kp, prep});
+      SplitJob bj{x.B, b_sr, b_sk, reinterpret_cast<__nv_bfloat16*>(base + b_off[j]), x.N, x.K, kp,
+                  prep};
+      if (gather) { bj.gather = gather; bj.im = *x.b_im2col; }
+      sjobs.push_back(bj);
       prep += cdiv(x.N, 32) * tk;
     }
   }
@@ -458,6 +481,10 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   *out = p;
   return UGEMM_OK;
 }
+
+}  // namespace ugemm
+
+extern "C" {
 
 UGEMM_API int ugemm_grouped_run(ugemm_grouped_plan* p, void* stream) {
   if (!p) return plan_fail(UGEMM_ERR_ARG, "NULL plan");

@@ -29,6 +29,48 @@ struct Epilogue {
   float slope = 0.1f;
 };
 
+// An operand read as the im2col matrix of a CNHW activation x without
+// materialising it (implicit GEMM): entry (tap, pix), tap = c*k*k + ki*k + kj,
+// pix = (b*Ho + i)*Wo + j, is x[c][b][i*stride - pad + ki][j*stride - pad + kj],
+// 0 outside the image -- the reference's im2col (sgemm_ocl1.h:81-119) for a
+// batch of images side by side.
+// Division by a run-time constant d >= 1 of 0 <= x < 2^31 with one
+// multiply-high, an add and a shift: q = (umulhi(x, m) + x) >> s with
+// s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1 (the round-up method of
+// Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994).
+struct FastDiv {
+  uint32_t d = 1, m = 1, s = 0;
+  FastDiv() = default;
+  explicit FastDiv(uint32_t div) : d(div) {
+    while ((uint64_t(1) << s) < div) ++s;
+    m = static_cast<uint32_t>(((uint64_t(1) << 32) * ((uint64_t(1) << s) - div)) / div + 1);
+  }
+#ifdef __CUDACC__
+  __device__ __forceinline__ int operator()(int x) const {
+    const uint32_t u = static_cast<uint32_t>(x);
+    return static_cast<int>((__umulhi(u, m) + u) >> s);
+  }
+#endif
+};
+
+struct Im2col {
+  const float* x = nullptr;
+  int C = 0, B = 0, H = 0, W = 0, k = 0, pad = 0, stride = 1, Ho = 0, Wo = 0;
+  FastDiv by_kk, by_k, by_hw, by_wo;  // k*k, k, Ho*Wo, Wo
+};
+inline Im2col make_im2col(const float* x, int C, int B, int H, int W, int k, int pad, int stride,
+                          int Ho, int Wo) {
+  Im2col g;
+  g.x = x;
+  g.C = C; g.B = B; g.H = H; g.W = W; g.k = k; g.pad = pad; g.stride = stride; g.Ho = Ho; g.Wo = Wo;
+  g.by_kk = FastDiv(static_cast<uint32_t>(k * k));
+  g.by_k = FastDiv(static_cast<uint32_t>(k));
+  g.by_hw = FastDiv(static_cast<uint32_t>(Ho * Wo));
+  g.by_wo = FastDiv(static_cast<uint32_t>(Wo));
+  return g;
+}
+
 struct Gemm {
   char ta, tb;
   int M, N, K;
@@ -40,6 +82,9 @@ struct Gemm {
   float* C;
   int ldc;
   Epilogue epi{};
+  // grouped plans only: B is the im2col matrix of b_im2col->x (K x N taps x
+  // pixels when tb == 'N', N x K when tb == 'T'); B and ldb are then unused
+  const Im2col* b_im2col = nullptr;
 };
 
 #ifdef __CUDACC__
@@ -47,6 +92,32 @@ __device__ __forceinline__ float epilogue_apply(float v, const Epilogue& e, int 
   if (e.bias) v += e.bias[row];
   if (e.act) v = v > 0.f ? v : v * e.slope;
   return v;
+}
+
+// An im2col row (tap) and column (pixel) as coordinates; consecutive pixels
+// step along j, then i, then b.
+struct Im2colTap { int c, ki, kj; };
+struct Im2colPix { int b, i, j; };
+
+__device__ __forceinline__ Im2colTap im2col_tap(const Im2col& g, int tap) {
+  const int c = g.by_kk(tap), t = tap - c * g.k * g.k, ki = g.by_k(t);
+  return Im2colTap{c, ki, t - ki * g.k};
+}
+__device__ __forceinline__ Im2colPix im2col_pix(const Im2col& g, int pix) {
+  const int b = g.by_hw(pix), q = pix - b * g.Ho * g.Wo, i = g.by_wo(q);
+  return Im2colPix{b, i, q - i * g.Wo};
+}
+__device__ __forceinline__ void im2col_next(const Im2col& g, Im2colPix& p) {
+  if (++p.j == g.Wo) {
+    p.j = 0;
+    if (++p.i == g.Ho) { p.i = 0; ++p.b; }
+  }
+}
+__device__ __forceinline__ float im2col_load(const Im2col& g, const Im2colTap& t,
+                                             const Im2colPix& p) {
+  const int yy = p.i * g.stride - g.pad + t.ki, xx = p.j * g.stride - g.pad + t.kj;
+  if (yy < 0 || yy >= g.H || xx < 0 || xx >= g.W) return 0.f;
+  return g.x[((static_cast<long long>(t.c) * g.B + p.b) * g.H + yy) * g.W + xx];
 }
 #endif
 
@@ -125,7 +196,12 @@ size_t multi_scratch_bytes(const Gemm* gs, int n, const SplitPlan& p);
 ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& p, Scratch ws, int* dev_err,
                           cudaStream_t st);
 
-// Grouped plans: default tile configuration and the autotuner's cache.
+// Grouped plans: the builder behind ugemm_grouped_plan_create (validated
+// problems, longest k first inside), default tile configuration and the
+// autotuner's cache.  config == nullptr: the default configuration.
+ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
+                                const ugemm_tile_config* config, int flags,
+                                ugemm_grouped_plan** out);
 ugemm_tile_config default_grouped_config(int form);
 bool tuned_config(int count, const ugemm_problem* problems, int precision, ugemm_tile_config* cfg);
 int split_default_chunk_kb();

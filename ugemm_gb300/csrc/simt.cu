@@ -438,7 +438,23 @@ __global__ void __launch_bounds__(256) pack_kmajor_batched_kernel(const PackJob*
   const int tiles_k = (j.K + 63) / 64;
   const int r0 = (local / tiles_k) * 32, k0 = (local % tiles_k) * 64;
   const int t = threadIdx.x;
-  if (j.sk == 1) {
+  if (j.gather) {  // implicit im2col: this thread's pixel is fixed, taps vary
+    const int pix = j.gather == 2 ? k0 + (t & 63) : r0 + (t & 31);
+    const Im2colPix px = im2col_pix(j.im, pix);
+    const int npix = j.gather == 2 ? j.K : j.rows;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (j.gather == 2) {  // rows are taps
+        const int rr = (t >> 6) + 4 * i, r = r0 + rr;
+        tile[rr][t & 63] = (r < j.rows && pix < npix) ? im2col_load(j.im, im2col_tap(j.im, r), px)
+                                                       : 0.f;
+      } else {              // rows are pixels
+        const int kk = (t >> 5) + 8 * i, k = k0 + kk;
+        tile[t & 31][kk] = (k < j.K && pix < npix) ? im2col_load(j.im, im2col_tap(j.im, k), px)
+                                                    : 0.f;
+      }
+    }
+  } else if (j.sk == 1) {
     const int k = k0 + (t & 63);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {

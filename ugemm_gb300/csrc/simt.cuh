@@ -44,6 +44,10 @@ struct PackJob {
   float* dst;
   int rows, K, ld;
   int tile_start;       // first 32 x 64 tile of this job
+  // implicit im2col operand (src unused): 1 = rows are pixels and k taps,
+  // 2 = rows are taps and k pixels; 0 = plain strided matrix
+  int gather = 0;
+  Im2col im;
 };
 
 ugemm_status simt_grouped_launch(int tile, const CUtensorMap* maps, const SimtProblem* probs,

@@ -502,6 +502,48 @@ struct RawTile {
 
 __device__ __forceinline__ void load_raw(const SplitJob& j, int r0, int k0, RawTile& out) {
   const int t = threadIdx.x;
+  if (j.gather) {  // implicit im2col: the same thread layout, gathered from x
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int idx = t + 256 * i;
+      // 4 consecutive pixels at one tap: rows are taps and k pixels (2), or
+      // rows are pixels and k taps (1)
+      int tap, pix, n;
+      if (j.gather == 2) {
+        const int rr = idx >> 4, c4 = (idx & 15) * 4;
+        tap = r0 + rr;
+        pix = k0 + c4;
+        n = tap < j.rows ? j.K - pix : 0;
+      } else {
+        const int kk = idx >> 3, q4 = (idx & 7) * 4;
+        tap = k0 + kk;
+        pix = r0 + q4;
+        n = tap < j.K ? j.rows - pix : 0;
+      }
+      // walk the image row: one address per row, a step of `stride` per pixel
+      const Im2colTap tp = im2col_tap(j.im, tap);
+      Im2colPix px = im2col_pix(j.im, pix);
+      int xx = px.j * j.im.stride - j.im.pad + tp.kj;
+      int yy = px.i * j.im.stride - j.im.pad + tp.ki;
+      const float* row = j.im.x + ((static_cast<long long>(tp.c) * j.im.B + px.b) * j.im.H + yy) *
+                                      static_cast<long long>(j.im.W);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        out.v[i][e] = (e < n && yy >= 0 && yy < j.im.H && xx >= 0 && xx < j.im.W) ? row[xx] : 0.f;
+        if (++px.j == j.im.Wo) {  // next image row (or image)
+          px.j = 0;
+          if (++px.i == j.im.Ho) { px.i = 0; ++px.b; }
+          xx = -j.im.pad + tp.kj;
+          yy = px.i * j.im.stride - j.im.pad + tp.ki;
+          row = j.im.x + ((static_cast<long long>(tp.c) * j.im.B + px.b) * j.im.H + yy) *
+                             static_cast<long long>(j.im.W);
+        } else {
+          xx += j.im.stride;
+        }
+      }
+    }
+    return;
+  }
   const bool kcontig = j.sk == 1;
   const long long other = kcontig ? j.sr : j.sk;
   const bool vec = ((reinterpret_cast<uintptr_t>(j.src) & 15) == 0) && ((other & 3) == 0);

@@ -63,6 +63,10 @@ struct SplitJob {
   __nv_bfloat16* dst;   // [pieces][rows][Kp]
   int rows, K, Kp;
   int tile_start;       // first 32x64 tile index of this job
+  // implicit im2col operand (src unused): 1 = rows are pixels and k taps,
+  // 2 = rows are taps and k pixels; 0 = plain strided matrix
+  int gather = 0;
+  Im2col im;
 };
 
 int split_kp(int K);
