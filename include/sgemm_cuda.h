@@ -237,8 +237,11 @@ UGEMM_API int ugemm_col2im(const float *col, int channels, int batch, int height
  *            dX_l = col2im(dcol_l) = dY_{l-1}
  * with X_{l+1} = Y_l.  By default the GEMMs read col_l = im2col(X_l)
  * implicitly: the operand pass of the forward and dW GEMMs gathers it from
- * X_l, and no col buffer exists.  UGEMM_CONV_IM2COL materialises col_l with
- * an im2col pass first (the reference's formulation) and keeps the buffer.  The gradient entering the last layer is its own
+ * X_l, and no col buffer exists; in the split forms a stride-1 layer's dX is
+ * then one GEMM, dX_l = Wt_l * im2col(dY_l, pad k-1-p) with Wt_l the weights
+ * transposed in the channels and flipped in the taps, and has no dcol
+ * buffer.  UGEMM_CONV_IM2COL materialises col_l with an im2col pass first
+ * and keeps dcol + col2im for every layer (the reference's formulation).  The gradient entering the last layer is its own
  * output (loss 0.5 * ||Y_last||^2).  With act == 1 a layer computes
  * Y_l = LeakyReLU(W_l * col_l + bias_l) in the GEMM epilogue
  * (gl_convolution_LReLU, sgemm_gl1.h:192-218), and its backward first scales
@@ -262,7 +265,7 @@ enum {
   UGEMM_CONV_Y = 2,
   UGEMM_CONV_COL = 3, /* UGEMM_CONV_IM2COL stacks only */
   UGEMM_CONV_DW = 4,
-  UGEMM_CONV_DCOL = 5,
+  UGEMM_CONV_DCOL = 5, /* not for the direct-dX layers of implicit stacks */
   UGEMM_CONV_DX = 6,
   UGEMM_CONV_DY = 7,
   UGEMM_CONV_BIAS = 8, /* cout floats, used when act == 1 (fill before running) */

@@ -98,6 +98,20 @@ dim3 plane_grid(int planes, int plane_px) {
 
 int out_dim(int in, int k, int pad, int stride) { return (in + 2 * pad - k) / stride + 1; }
 
+// wt[c][(co*k + k-1-ki)*k + k-1-kj] = w[co][(c*k + ki)*k + kj]: the weights of
+// the adjoint (transposed) convolution of a stride-1 layer.
+__global__ void flip_weights_kernel(const float* __restrict__ w, int cout, int cin, int k,
+                                    float* __restrict__ wt) {
+  const int kk = k * k;
+  const int total = cout * cin * kk;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += gridDim.x * blockDim.x) {
+    const int co = idx / (cin * kk), rem = idx - co * cin * kk;
+    const int c = rem / kk, t = rem - c * kk, ki = t / k, kj = t - ki * k;
+    wt[(static_cast<long long>(c) * cout + co) * kk + (k - 1 - ki) * k + (k - 1 - kj)] = w[idx];
+  }
+}
+
 // Backward of the fused epilogue Y = LeakyReLU(W*col + bias): the incoming
 // gradient dY (C x n, in place) is multiplied by the activation's slope
 // where Y <= 0, and dbias[c] = sum over the row of the masked gradient.  One
@@ -142,6 +156,15 @@ ugemm_status im2col_launch(const float* x, int C, int B, int H, int W, int k, in
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
 
+ugemm_status flip_weights_launch(const float* w, int cout, int cin, int k, float* wt,
+                                cudaStream_t st) {
+  const int total = cout * cin * k * k;
+  prof_begin(st);
+  flip_weights_kernel<<<std::min(cdiv(total, 256), 1024), 256, 0, st>>>(w, cout, cin, k, wt);
+  prof_end(st, kProfAux);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
 ugemm_status col2im_launch(const float* col, int C, int B, int H, int W, int k, int pad,
                            int stride, float* dx, cudaStream_t st) {
   const int Ho = out_dim(H, k, pad, stride), Wo = out_dim(W, k, pad, stride);
@@ -170,6 +193,11 @@ struct ugemm_conv_stack_s {
     float *x, *col, *w, *y, *dw, *dcol, *dx;  // dy of layer l is dx of layer l+1
     float *bias = nullptr, *dbias = nullptr;  // act == 1 only
     ugemm::Im2col im;     // im2col geometry of x (the implicit operand)
+    // implicit stacks, stride 1: dX as one GEMM, the convolution of dY with
+    // the flipped, transposed weights wt (no dcol, no col2im)
+    bool direct_dx = false;
+    float* wt = nullptr;  // cin x cout*k*k
+    ugemm::Im2col dy_im;  // im2col geometry of dY for that GEMM
     ugemm_grouped_plan* fwd = nullptr;
     ugemm_grouped_plan* bwd = nullptr;
   };
@@ -210,11 +238,17 @@ int run_stack(Stack* s, int what, cudaStream_t st) {
         prof_end(st, kProfAux);
         if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
       }
+      if (L.direct_dx) {
+        ugemm_status r = flip_weights_launch(L.w, L.d.cout, L.d.cin, L.d.ksize, L.wt, st);
+        if (r != UGEMM_OK) return r;
+      }
       int rc = ugemm_grouped_run(L.bwd, st);
       if (rc != UGEMM_OK) return rc;
-      ugemm_status r = col2im_launch(L.dcol, L.d.cin, s->batch, L.d.height, L.d.width,
-                                     L.d.ksize, L.d.pad, L.d.stride, L.dx, st);
-      if (r != UGEMM_OK) return r;
+      if (!L.direct_dx) {
+        ugemm_status r = col2im_launch(L.dcol, L.d.cin, s->batch, L.d.height, L.d.width,
+                                       L.d.ksize, L.d.pad, L.d.stride, L.dx, st);
+        if (r != UGEMM_OK) return r;
+      }
     }
   }
   return UGEMM_OK;
@@ -294,6 +328,10 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     }
     L.n = static_cast<long long>(batch) * L.Ho * L.Wo;
     L.kdim = d.cin * d.ksize * d.ksize;
+    // (split forms only: the SIMT form's K-major pack of the 9x wider
+    // gathered dY costs more than dcol + col2im, measured)
+    L.direct_dx = !s->explicit_col && s->form != UGEMM_PREC_SIMT && d.stride == 1 &&
+                  d.pad <= d.ksize - 1;
     if (L.n > 0x7fffffffLL) { destroy_stack(s); return UGEMM_ERR_ARG; }
     s->layers.push_back(L);
   }
@@ -304,7 +342,8 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     off.push_back(take(size_t(L.d.cout) * L.kdim));            // w
     off.push_back(take(size_t(L.d.cout) * L.n));               // y
     off.push_back(take(size_t(L.d.cout) * L.kdim));            // dw
-    off.push_back(take(size_t(L.kdim) * L.n));                 // dcol
+    off.push_back(L.direct_dx ? take(size_t(L.d.cout) * L.kdim)   // wt
+                              : take(size_t(L.kdim) * L.n));      // dcol
     off.push_back(take(size_t(L.d.cin) * batch * L.d.height * L.d.width));  // dx
     off.push_back(take(size_t(L.d.cout)));                     // bias
     off.push_back(take(size_t(L.d.cout)));                     // dbias
@@ -320,7 +359,8 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     L.w = at(off[8 * l + 1]);
     L.y = at(off[8 * l + 2]);
     L.dw = at(off[8 * l + 3]);
-    L.dcol = at(off[8 * l + 4]);
+    L.dcol = L.direct_dx ? nullptr : at(off[8 * l + 4]);
+    L.wt = L.direct_dx ? at(off[8 * l + 4]) : nullptr;
     L.dx = at(off[8 * l + 5]);
     L.bias = at(off[8 * l + 6]);
     L.dbias = at(off[8 * l + 7]);
@@ -343,11 +383,23 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
     Gemm f{'N', 'N', M, N, K, 1.f, 0.f, L.w, K, L.col, N, L.y, N};
     f.epi = Epilogue{L.d.act ? L.bias : nullptr, L.d.act, L.d.slope};
     f.b_im2col = im;
-    // backward: dw = dy * col^T, dcol = w^T * dy
+    // backward: dw = dy * col^T, and dcol = w^T * dy (dX = col2im(dcol)) or,
+    // for a direct layer, dX = wt * im2col(dY; pad k-1-p): the adjoint of a
+    // stride-1 convolution is the convolution of dY with the weights
+    // transposed in the channels and flipped in the taps
     const float* g = dy ? dy : L.y;
     Gemm b[2] = {Gemm{'N', 'T', M, K, N, 1.f, 0.f, g, N, L.col, N, L.dw, K},
                  Gemm{'T', 'N', K, N, M, 1.f, 0.f, L.w, K, g, N, L.dcol, N}};
     b[0].b_im2col = im;
+    if (L.direct_dx) {
+      const int kk = L.d.ksize * L.d.ksize;
+      const int npix = batch * L.d.height * L.d.width;
+      L.dy_im = make_im2col(g, L.d.cout, batch, L.Ho, L.Wo, L.d.ksize, L.d.ksize - 1 - L.d.pad, 1,
+                            L.d.height, L.d.width);
+      b[1] = Gemm{'N', 'N', L.d.cin, npix, L.d.cout * kk, 1.f, 0.f, L.wt, L.d.cout * kk, nullptr,
+                  npix, L.dx, npix};
+      b[1].b_im2col = &L.dy_im;
+    }
     ugemm_status rc = grouped_plan_build(&f, 1, s->form, nullptr, 0, &L.fwd);
     if (rc == UGEMM_OK) rc = grouped_plan_build(b, 2, s->form, nullptr, 0, &L.bwd);
     if (rc != UGEMM_OK) { destroy_stack(s); return rc; }
@@ -392,7 +444,11 @@ UGEMM_API int ugemm_conv_stack_buffer(ugemm_conv_stack* s, int layer, int which,
       n = size_t(L.kdim) * L.n;
       break;
     case UGEMM_CONV_DW: *ptr = L.dw; n = size_t(L.d.cout) * L.kdim; break;
-    case UGEMM_CONV_DCOL: *ptr = L.dcol; n = size_t(L.kdim) * L.n; break;
+    case UGEMM_CONV_DCOL:
+      if (L.direct_dx) return UGEMM_ERR_UNSUPPORTED;  // dX computed without dcol
+      *ptr = L.dcol;
+      n = size_t(L.kdim) * L.n;
+      break;
     case UGEMM_CONV_DX: *ptr = L.dx; n = x_n; break;
     case UGEMM_CONV_BIAS: *ptr = L.bias; n = L.d.cout; break;
     case UGEMM_CONV_DBIAS: *ptr = L.dbias; n = L.d.cout; break;
