@@ -239,7 +239,9 @@ def conv_forms(ug, torch, stream, steps):
 
 def profile_case(args):
     """One kernel family on a size ncu can capture (no timing, no JSON line):
-    'split'/'simt' = size^3 NN SGEMM; 'grouped_*' = the 256-problem group."""
+    'split'/'simt' = size^3 NN SGEMM; 'grouped_*' = the 256-problem group;
+    'conv_split' = the 12-layer conv stack (implicit im2col, split form) at
+    batch --size (16: operands above L2, about 2 GB on the device)."""
     import torch
 
     import ugemm_gb300 as ug
@@ -248,7 +250,17 @@ def profile_case(args):
     ug.load()
     n = args.size
     reps = max(1, args.steps)
-    if args.profile_case in ("split", "simt"):
+    if args.profile_case == "conv_split":
+        layers = workloads.conv_layers(n)
+        st = ug.ConvStack(layers, n, precision="bf16x6", graph=False)
+        cin, _, h, w, _ = layers[0]
+        st.tensor(0, "x", (cin, n * h * w)).uniform_()
+        for l, (ci, co, _, _, _) in enumerate(layers):
+            st.tensor(l, "w", (co, ci * 9)).normal_(0.0, (2.0 / (ci * 9)) ** 0.5)
+        for _ in range(reps):
+            st.run()
+        st.close()
+    elif args.profile_case in ("split", "simt"):
         A = torch.rand((n, n), device="cuda") * 2 - 1
         B = torch.rand((n, n), device="cuda") * 2 - 1
         C = torch.zeros((n, n), device="cuda")
@@ -302,7 +314,7 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--profile-case", default=None,
-                    choices=["split", "simt", "grouped_split", "grouped_simt"],
+                    choices=["split", "simt", "grouped_split", "grouped_simt", "conv_split"],
                     help="run only this case --steps times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -209,10 +209,13 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   } else {
     p->cfg = default_grouped_config(form);
     // Untuned split plans: 256-wide tiles only pay when the problems are wide
-    // (measured: 128 wins on the 256-problem set with N in [32, 1024]).
+    // in the orientation the kernel computes them (a transposed problem's
+    // width is its M): measured, 128 wins on the 256-problem set with N in
+    // [32, 1024] and on the conv stack, whose GEMMs are 64-512 wide.
     if (form != UGEMM_PREC_SIMT) {
       double n_sum = 0;
-      for (const Gemm& x : g) n_sum += x.N;
+      for (const Gemm& x : g)
+        n_sum += padded_area(x.N, x.M, 128) < padded_area(x.M, x.N, 128) ? x.M : x.N;
       if (n_sum / count < 512) p->cfg.block_n = 128;
     }
   }
