@@ -66,6 +66,8 @@ def load() -> ctypes.CDLL:
         lib.oracle_sgemm_avx256_mt.argtypes = [_i, _c, _c, _i, _i, _i, _f, _f32p, _i, _f32p, _i,
                                                _f, _f32p, _i]
         lib.oracle_sgemm_avx256_mt.restype = _i
+        lib.oracle_sgemm_sse.argtypes = _gemm_sig(_f32p, _f)
+        lib.oracle_sgemm_sse.restype = None
         lib.oracle_cmp_results.argtypes = [_i, _i, _f32p, _f32p, _i, _f64p]
         lib.oracle_cmp_results.restype = _i
         lib.oracle_im2col.argtypes = [_f32p, _i, _i, _i, _i, _i, _i, _f32p]

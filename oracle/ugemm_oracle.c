@@ -17,6 +17,7 @@
  *   oracle_dgemm_c        gemm_cpu.h:238-363 (via ugemm.h:29-33) FP64 of the above
  *   oracle_sgemm_avx256   sgemm_avx256.h:308-390 35x96 B-block, 2x24 core (NN)
  *   oracle_sgemm_avx256_mt  band-parallel harness around the above (all trans)
+ *   oracle_sgemm_sse      sgemm_sse.h:20-451   Goto-style blocks, 8x8 AVX tiles (all trans)
  *   oracle_cmp_results    check_sgemm.c:56-85  stdErr/stdRef/maxErr metric
  *   oracle_im2col         sgemm_ocl1.h:81-119  im2col (one image, square kernel)
  *   oracle_saxpy_cpu      ugemm.h:86-97        y += alpha*x with strides
@@ -210,6 +211,104 @@ int oracle_cmp_results(int M, int N, const float *ref, const float *res, int ld,
     if (max_err > std_ref * 1e-5) return 2;
     if (max_err > std_ref * 3e-5 || std_err > std_ref * 1e-6) return 1;
     return 0;
+}
+
+/*
+ * sgemm_sse.h:20-451 (sgemm_sse): a Goto-style SGEMM.  C is updated in blocks
+ * of 4096 columns x 384 k x 384 rows, each block in 8 x 8 tiles; a tile's
+ * product over one k block is, per element, a chain of multiply-adds from
+ * zero over k, fused as the reference's AVX kernel (sgemm_sse.h:106-170) is
+ * when built with FMA contraction (its Makefile).  Then per tile, with
+ * beta' = beta for the first k block and 1 for the others:
+ *   full 8 x 8 tile (sgemm_sse.h:204-232):  C = 0 (beta' == 0) or C *= beta'
+ *     (beta' != 1); C += AB (alpha == 1) or C = fma(alpha, AB, C);
+ *   edge tile (sgemm_sse.h:329-333):        T = alpha * AB; C *= beta' (or 0
+ *     when beta' == 0); C += T.
+ * The alpha == 0 shortcut (sgemm_sse.h:383-397) indexes C column-major
+ * whatever the major, as the reference does.
+ */
+#define SSE_MC 384
+#define SSE_KC 384
+#define SSE_NC 4096
+
+static void sse_scale(int m, int n, float beta, float *C, long cr, long cc)
+{
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < m; ++i)
+            C[i * cr + j * cc] = beta != 0.0f ? C[i * cr + j * cc] * beta : 0.0f;
+}
+
+static void sse_nn(int m, int n, int k, float alpha, const float *A, long ar, long ac,
+                   const float *B, long br, long bc, float beta, float *C, long cr, long cc)
+{
+    if (alpha == 0.0f || k == 0) {
+        sse_scale(m, n, beta, C, cr, cc);
+        return;
+    }
+    float ab[64];
+    for (int j0 = 0; j0 < n; j0 += SSE_NC) {
+        const int nc = n - j0 < SSE_NC ? n - j0 : SSE_NC;
+        for (int l0 = 0; l0 < k; l0 += SSE_KC) {
+            const int kc = k - l0 < SSE_KC ? k - l0 : SSE_KC;
+            const float bp = l0 == 0 ? beta : 1.0f;
+            for (int i0 = 0; i0 < m; i0 += SSE_MC) {
+                const int mc = m - i0 < SSE_MC ? m - i0 : SSE_MC;
+                for (int tj = 0; tj < nc; tj += 8) {
+                    for (int ti = 0; ti < mc; ti += 8) {
+                        const int mr = mc - ti < 8 ? mc - ti : 8, nr = nc - tj < 8 ? nc - tj : 8;
+                        const float *a = A + (long)(i0 + ti) * ar + (long)l0 * ac;
+                        const float *b = B + (long)l0 * br + (long)(j0 + tj) * bc;
+                        float *c = C + (long)(i0 + ti) * cr + (long)(j0 + tj) * cc;
+                        for (int j = 0; j < nr; ++j)
+                            for (int i = 0; i < mr; ++i) {
+                                float s = 0.0f;
+                                for (int l = 0; l < kc; ++l)
+                                    s = fmaf(a[i * ar + l * ac], b[l * br + j * bc], s);
+                                ab[i + 8 * j] = s;
+                            }
+                        for (int j = 0; j < nr; ++j)
+                            for (int i = 0; i < mr; ++i) {
+                                float *e = &c[i * cr + j * cc];
+                                const float p = ab[i + 8 * j];
+                                if (mr == 8 && nr == 8) {
+                                    float v = *e;
+                                    if (bp == 0.0f) v = 0.0f;
+                                    else if (bp != 1.0f) v = v * bp;
+                                    *e = alpha == 1.0f ? v + p : fmaf(alpha, p, v);
+                                } else {
+                                    const float t = alpha == 1.0f ? p : alpha * p;
+                                    const float v = bp != 0.0f ? *e * bp : 0.0f;
+                                    *e = v + t;
+                                }
+                            }
+                    }
+                }
+            }
+        }
+    }
+}
+
+void oracle_sgemm_sse(char major, char ta, char tb, int m, int n, int k, float alpha,
+                      const float *A, int lda, const float *B, int ldb, float beta, float *C,
+                      int ldc)
+{
+    if (m == 0 || n == 0 || ((alpha == 0.0f || k == 0) && beta == 1.0f)) return;
+    if (alpha == 0.0f) {
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < m; ++i)
+                C[i + (long)j * ldc] = beta == 0.0f ? 0.0f : C[i + (long)j * ldc] * beta;
+        return;
+    }
+    const int tA = ta == 'T', tB = tb == 'T';
+    if (major == 'C') {
+        /* column-major: A(i, l) at A[i + l*lda] ('N') or A[l + i*lda] ('T') */
+        sse_nn(m, n, k, alpha, A, tA ? lda : 1, tA ? 1 : lda, B, tB ? ldb : 1, tB ? 1 : ldb, beta,
+               C, 1, ldc);
+    } else {
+        /* row-major: A(i, l) at A[i*lda + l] ('N') or A[l*lda + i] ('T') */
+        sse_nn(m, n, k, alpha, A, tA ? 1 : lda, tA ? lda : 1, B, tB ? 1 : ldb, tB ? ldb : 1, beta,
+               C, ldc, 1);
+    }
 }
 
 /*

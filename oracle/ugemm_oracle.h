@@ -26,6 +26,9 @@ void oracle_sgemm_avx256(int M, int N, int K, float alpha, const float *A, int l
 int oracle_sgemm_avx256_mt(int nthreads, char ta, char tb, int M, int N, int K, float alpha,
                            const float *A, int lda, const float *B, int ldb, float beta,
                            float *C, int ldc);
+void oracle_sgemm_sse(char major, char ta, char tb, int m, int n, int k, float alpha,
+                      const float *A, int lda, const float *B, int ldb, float beta, float *C,
+                      int ldc);
 int oracle_cmp_results(int M, int N, const float *ref, const float *res, int ld, double out[4]);
 void oracle_im2col(const float *im, int channels, int height, int width, int ksize, int pad,
                    int stride, float *col);

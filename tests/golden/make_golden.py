@@ -8,6 +8,7 @@ calls the reference functions through ctypes:
 * ``sgemm_c``    (gemm_cpu.h:284) the same cases, K up to 800 (KC=384 blocks)
 * ``sgemm_avx``  (sgemm_avx256.h:392) NN row-major, N and K across the 96/35
   block edges
+* ``sgemm_sse`` (sgemm_sse.h:400) 8x8-tile Goto GEMM, both majors, all transposes
 * ``dgemm_cpu`` / ``_dgemm_c`` / ``dgemm_avx`` (ugemm.h:162, gemm_cpu.h:284,
   dgemm_avx.h:844) FP64
 * ``cmp_results`` (check_sgemm.c:56) printed lines
@@ -148,6 +149,23 @@ def main() -> None:
         strict.sgemv_cpu(trans.encode(), M, N, 1.5, A, lda, x, inc, 0.5, yr, inc)
         add(f"gemv/{i}", A=A, x=x, y=y, flags=np.frombuffer(trans.encode(), dtype=np.uint8),
             meta=np.array([M, N, lda, inc], dtype=np.int64), out=yr)
+
+    # --- sgemm_sse (sgemm_sse.h:400-451), built with contraction like the
+    # reference: two k blocks (k = 400 > 384) in every major/transpose
+    # combination, and two row blocks (m = 390 > 384) with edge tiles
+    sse_cases = [(major, ta, tb, 13, 11, 400, 1.5, 0.5) for major in "RC" for ta in "NT"
+                 for tb in "NT"]
+    sse_cases += [("R", "N", "N", 390, 9, 20, 1.0, 0.0), ("C", "T", "N", 390, 9, 20, 0.75, 1.0)]
+    for n_case, (major, ta, tb, M, N, K, alpha, beta) in enumerate(sse_cases):
+        A = rng.uniform(-1, 1, stored(major, ta, M, K)).astype(np.float32)
+        B = rng.uniform(-1, 1, stored(major, tb, K, N)).astype(np.float32)
+        C = rng.uniform(-1, 1, (M, N) if major == "R" else (N, M)).astype(np.float32)
+        Cr = C.copy()
+        fast.ref_sgemm_sse(major.encode(), ta.encode(), tb.encode(), M, N, K, alpha, A, A.shape[1],
+                           B, B.shape[1], beta, Cr, Cr.shape[1])
+        add(f"sse/{n_case}", A=A, B=B, C=C, meta=np.array([M, N, K], dtype=np.int64),
+            ab=np.array([alpha, beta], dtype=np.float32),
+            flags=np.frombuffer((major + ta + tb).encode(), dtype=np.uint8), sgemm_sse=Cr)
 
     # --- known-answer test, sgemm_test.c:186-200 (RNN 3x3x2)
     A = np.array([[1, 2], [3, 4], [5, 6]], dtype=np.float32)

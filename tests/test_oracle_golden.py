@@ -18,8 +18,8 @@ def _cases(golden, prefix):
 def test_oracle_builds_and_loads():
     lib = oracle.load()
     for sym in ("oracle_sgemm_cpu", "oracle_dgemm_cpu", "oracle_sgemm_c", "oracle_dgemm_c",
-                "oracle_sgemm_avx256", "oracle_sgemm_avx256_mt", "oracle_cmp_results",
-                "oracle_im2col"):
+                "oracle_sgemm_avx256", "oracle_sgemm_avx256_mt", "oracle_sgemm_sse",
+                "oracle_cmp_results", "oracle_im2col"):
         assert hasattr(lib, sym)
 
 
@@ -48,6 +48,23 @@ def test_avx256_port_bit_exact(golden):
         C = g("C").copy()
         lib.oracle_sgemm_avx256(M, N, K, alpha, g("A"), K, g("B"), N, beta, C, N)
         assert np.array_equal(C, g("sgemm_avx")), name
+
+
+def test_sse_goto_gemm_bit_exact(golden):
+    """sgemm_sse (sgemm_sse.h:400-451): both majors, all transposes, two k
+    blocks, two row blocks, edge tiles, alpha/beta special cases."""
+    cases = _cases(golden, "sse/")
+    assert len(cases) >= 10
+    lib = oracle.load()
+    for name in cases:
+        g = lambda k: golden[f"{name}/{k}"]  # noqa: E731
+        M, N, K = (int(x) for x in g("meta"))
+        alpha, beta = (float(x) for x in g("ab"))
+        major, ta, tb = bytes(g("flags")).decode()
+        A, B, C = g("A"), g("B"), g("C").copy()
+        lib.oracle_sgemm_sse(major.encode(), ta.encode(), tb.encode(), M, N, K, alpha, A,
+                             A.shape[1], B, B.shape[1], beta, C, C.shape[1])
+        assert np.array_equal(C, g("sgemm_sse")), name
 
 
 @pytest.mark.parametrize("threads", [1, 3, 4])
