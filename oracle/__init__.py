@@ -68,6 +68,9 @@ def load() -> ctypes.CDLL:
         lib.oracle_sgemm_avx256_mt.restype = _i
         lib.oracle_sgemm_sse.argtypes = _gemm_sig(_f32p, _f)
         lib.oracle_sgemm_sse.restype = None
+        for name in ("oracle_gemm_rnn", "oracle_gemm_rnt", "oracle_gemm_rtn"):
+            getattr(lib, name).argtypes = [_i, _i, _i, _f, _f32p, _f32p, _f, _f32p]
+            getattr(lib, name).restype = None
         lib.oracle_cmp_results.argtypes = [_i, _i, _f32p, _f32p, _i, _f64p]
         lib.oracle_cmp_results.restype = _i
         lib.oracle_im2col.argtypes = [_f32p, _i, _i, _i, _i, _i, _i, _f32p]

@@ -18,6 +18,7 @@
  *   oracle_sgemm_avx256   sgemm_avx256.h:308-390 35x96 B-block, 2x24 core (NN)
  *   oracle_sgemm_avx256_mt  band-parallel harness around the above (all trans)
  *   oracle_sgemm_sse      sgemm_sse.h:20-451   Goto-style blocks, 8x8 AVX tiles (all trans)
+ *   oracle_gemm_rnn/rnt/rtn  sgemm_test.c:40-105  the GPU test's CPU loops (tight ld)
  *   oracle_cmp_results    check_sgemm.c:56-85  stdErr/stdRef/maxErr metric
  *   oracle_im2col         sgemm_ocl1.h:81-119  im2col (one image, square kernel)
  *   oracle_saxpy_cpu      ugemm.h:86-97        y += alpha*x with strides
@@ -309,6 +310,59 @@ void oracle_sgemm_sse(char major, char ta, char tb, int m, int n, int k, float a
         sse_nn(m, n, k, alpha, A, tA ? 1 : lda, tA ? lda : 1, B, tB ? 1 : ldb, tB ? ldb : 1, beta,
                C, ldc, 1);
     }
+}
+
+/*
+ * sgemm_test.c:40-105: the CPU loops the reference's GPU test checks its
+ * kernels against, row-major with tight leading dimensions.  C is first
+ * zeroed (beta == 0) or scaled (beta != 1); then
+ *   rnn (A M x K, B K x N) and rtn (A stored K x M): for each row m and each
+ *     k in order, a = alpha * A(m, k) rounded, then C(m, n) += a * B(k, n);
+ *   rnt (B stored N x K): C(m, n) += alpha * (sum over k in order of A(m, k)
+ *     * B(n, k), accumulated in float).
+ * sgemm_test.c itself needs the OpenCL headers and cannot be compiled here;
+ * these restatements are pinned by the tests (exact integer inputs against
+ * oracle_sgemm_cpu, and the known-answer test).
+ */
+static void gemm_beta(int M, int N, float beta, float *C)
+{
+    if (beta == 0.0f) memset(C, 0, sizeof(float) * (size_t)M * N);
+    else if (beta != 1.0f)
+        for (long i = 0; i < (long)M * N; ++i) C[i] *= beta;
+}
+
+void oracle_gemm_rnn(int M, int N, int K, float alpha, const float *A, const float *B, float beta,
+                     float *C)
+{
+    gemm_beta(M, N, beta, C);
+    for (int m = 0; m < M; ++m)
+        for (int k = 0; k < K; ++k) {
+            const float a = alpha * A[(long)m * K + k];
+            for (int n = 0; n < N; ++n) C[(long)m * N + n] += a * B[(long)k * N + n];
+        }
+}
+
+void oracle_gemm_rtn(int M, int N, int K, float alpha, const float *A, const float *B, float beta,
+                     float *C)
+{
+    gemm_beta(M, N, beta, C);
+    for (int m = 0; m < M; ++m)
+        for (int k = 0; k < K; ++k) {
+            const float a = alpha * A[m + (long)M * k];
+            for (int n = 0; n < N; ++n) C[(long)m * N + n] += a * B[(long)k * N + n];
+        }
+}
+
+void oracle_gemm_rnt(int M, int N, int K, float alpha, const float *A, const float *B, float beta,
+                     float *C)
+{
+    gemm_beta(M, N, beta, C);
+    for (int m = 0; m < M; ++m)
+        for (int n = 0; n < N; ++n) {
+            float sum = 0.0f;
+            for (int k = 0; k < K; ++k) sum += A[(long)m * K + k] * B[k + (long)K * n];
+            C[(long)m * N + n] += alpha * sum;
+        }
 }
 
 /*

@@ -29,6 +29,12 @@ int oracle_sgemm_avx256_mt(int nthreads, char ta, char tb, int M, int N, int K, 
 void oracle_sgemm_sse(char major, char ta, char tb, int m, int n, int k, float alpha,
                       const float *A, int lda, const float *B, int ldb, float beta, float *C,
                       int ldc);
+void oracle_gemm_rnn(int M, int N, int K, float alpha, const float *A, const float *B, float beta,
+                     float *C);
+void oracle_gemm_rnt(int M, int N, int K, float alpha, const float *A, const float *B, float beta,
+                     float *C);
+void oracle_gemm_rtn(int M, int N, int K, float alpha, const float *A, const float *B, float beta,
+                     float *C);
 int oracle_cmp_results(int M, int N, const float *ref, const float *res, int ld, double out[4]);
 void oracle_im2col(const float *im, int channels, int height, int width, int ksize, int pad,
                    int stride, float *col);

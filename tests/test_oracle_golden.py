@@ -67,6 +67,30 @@ def test_sse_goto_gemm_bit_exact(golden):
         assert np.array_equal(C, g("sgemm_sse")), name
 
 
+@pytest.mark.parametrize("loop,ta,tb", [("rnn", "N", "N"), ("rnt", "N", "T"), ("rtn", "T", "N")])
+def test_gpu_test_cpu_loops(golden, loop, ta, tb):
+    """sgemm_test.c:40-105 (not compilable here: it needs OpenCL headers).
+    On small-integer inputs every product and sum is exact in FP32, so the
+    loops must equal the naive oracle exactly whatever their order; plus the
+    known-answer test of sgemm_test.c:186-200 through gemm_rnn."""
+    lib = oracle.load()
+    rng = np.random.default_rng(7)
+    M, N, K = 23, 17, 31
+    A = rng.integers(-8, 9, oracle.op_shape(ta, M, K)).astype(np.float32)
+    B = rng.integers(-8, 9, oracle.op_shape(tb, K, N)).astype(np.float32)
+    for alpha, beta in ((1.0, 0.0), (2.0, 0.5), (1.0, 1.0)):
+        C0 = rng.integers(-8, 9, (M, N)).astype(np.float32)
+        got = C0.copy()
+        getattr(lib, f"oracle_gemm_{loop}")(M, N, K, alpha, A, B, beta, got)
+        ref = oracle.sgemm("oracle_sgemm_cpu", ta, tb, M, N, K, alpha, A, B, beta, C0.copy())
+        assert np.array_equal(got, ref), (loop, alpha, beta)
+    if loop == "rnn":
+        g = lambda k: golden[f"kat/rnn3x3x2/{k}"]  # noqa: E731
+        C = np.zeros((3, 3), dtype=np.float32)
+        lib.oracle_gemm_rnn(3, 3, 2, 1.0, g("A"), g("B"), 0.0, C)
+        assert np.array_equal(C, g("out"))
+
+
 @pytest.mark.parametrize("threads", [1, 3, 4])
 def test_avx256_threaded_harness_matches_single(golden, threads):
     """Row bands do not change per-element arithmetic; transposes are exact."""
