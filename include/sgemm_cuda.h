@@ -309,6 +309,15 @@ UGEMM_API int ugemm_sgemv(char trans, int M, int N, float alpha, const float *A,
 UGEMM_API int ugemm_profile_enable(int on);
 UGEMM_API int ugemm_profile_collect(double *ms_per_kind, int *launches_per_kind, int nkinds);
 
+/* Failure-detection self-test (no reference counterpart; the reference's
+ * OpenCL calls have no device-side failure detection).  Runs one small
+ * kernel whose threads wait, through the library's bounded mbarrier wait with
+ * a 100 ms limit, on a barrier nothing arrives on.  Returns
+ * UGEMM_ERR_TIMEOUT with the recorded device error code (1: a pipeline stage
+ * never filled), the number of threads that gave up and returned, and the
+ * wall time; the CUDA context stays usable.  Faults, traps and hangs nothing. */
+UGEMM_API int ugemm_selftest_wait_timeout(int *code, int *threads_returned, double *seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -275,6 +275,17 @@ def profile_collect() -> dict:
     return {k: (ms[i], cnt[i]) for i, k in enumerate(PROF_KINDS)}
 
 
+def selftest_wait_timeout():
+    """Run the bounded-wait self-test; returns (status, code, threads, seconds)."""
+    lib = load()
+    lib.ugemm_selftest_wait_timeout.argtypes = [ctypes.POINTER(_i), ctypes.POINTER(_i),
+                                                ctypes.POINTER(ctypes.c_double)]
+    code, threads, secs = _i(), _i(), ctypes.c_double()
+    st = lib.ugemm_selftest_wait_timeout(ctypes.byref(code), ctypes.byref(threads),
+                                         ctypes.byref(secs))
+    return st, code.value, threads.value, secs.value
+
+
 # --------------------------------------------------------------------------
 # Grouped GEMM and autotuner
 # --------------------------------------------------------------------------

@@ -81,6 +81,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Wait for the phase with the given parity to complete.  Returns false (and
 // records `code`) if the wait exceeded kWaitLimitNs or another thread of the
 // grid already recorded an error.
+// (The limit is a template parameter only so that the failure self-test can
+// exercise this same loop with a short limit.)
+template <uint64_t kLimitNs = kWaitLimitNs>
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
@@ -88,7 +91,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* e
   while (!mbar_try_wait(bar, parity)) {
     if ((++spins & 255u) == 0) {
       if (error_raised(err)) return false;
-      if (globaltimer() - t0 > kWaitLimitNs) {
+      if (globaltimer() - t0 > kLimitNs) {
         record_error(err, code);
         return false;
       }
