@@ -4,6 +4,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -170,6 +171,22 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
 SplitPlan split_plan_for(int precision, const Gemm& g);
 
 // --- small helpers -----------------------------------------------------
+// Raise a kernel's dynamic shared-memory limit on the current device, once
+// per device (the attribute belongs to the device's context).  `done` is the
+// caller's per-kernel record of devices already set; a race only repeats an
+// idempotent call.
+template <typename Kernel>
+bool smem_attr_once(Kernel kern, size_t bytes, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  const uint64_t bit = uint64_t(1) << dev;
+  if (done.load(std::memory_order_acquire) & bit) return true;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(bytes)) != cudaSuccess)
+    return false;
+  done.fetch_or(bit, std::memory_order_release);
+  return true;
+}
 ugemm_status scale_c_launch(const Gemm& g, cudaStream_t st);  // C = beta*C (or 0)
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }

@@ -536,13 +536,8 @@ ugemm_status launch_t(const Gemm& g, const float* A, int lda, const float* B, in
   if constexpr (NP) kern = simt_sgemm_np_kernel<TM, TN, AK, BKM>;
   else kern = simt_sgemm_kernel<TM, TN, AK, BKM>;
   const int threads = NP ? kConsumerWarps * 32 : kThreads;
-  static bool attr_set = false;  // per instantiation
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(S::SMEM)) != cudaSuccess)
-      return UGEMM_ERR_CUDA;
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
+  if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
   const int tiles_m = cdiv(g.M, S::BM), tiles_n = cdiv(g.N, S::BN);
   prof_begin(st);
   kern<<<tiles_m * tiles_n, threads, S::SMEM, st>>>(ta, tb, g.C, g.M, g.N, g.K, g.ldc, g.alpha,
@@ -656,13 +651,8 @@ ugemm_status grouped_t(const CUtensorMap* maps, const SimtProblem* probs, int np
                        int max_ctas, int* dev_err, cudaStream_t st) {
   using S = SimtShape<TM, TN>;
   auto kern = simt_grouped_kernel<TM, TN>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(S::SMEM)) != cudaSuccess)
-      return UGEMM_ERR_CUDA;
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
+  if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
   int sms = 148, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

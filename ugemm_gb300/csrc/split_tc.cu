@@ -712,13 +712,8 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
                            cudaStream_t st) {
   using S = TcShape<NP, BN>;
   auto kern = split_tc_kernel<NP, BN, GROUPED, EPI>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(S::SMEM)) != cudaSuccess)
-      return UGEMM_ERR_CUDA;
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
+  if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
   const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
   kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, nprob, total_tiles, nprod,
