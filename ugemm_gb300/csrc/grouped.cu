@@ -73,6 +73,8 @@ struct ugemm_grouped_plan_s {
   int njobs = 0, prep_tiles = 0, gemm_tiles = 0;
   int nsub = 0;                   // kernel problems (split-K slices count one each)
   const void* reduce = nullptr;   // split-K reduce jobs
+  const int4* tiles = nullptr;    // split form: per-CTA ranges, then one record per tile
+  int grid = 0;                   // split form: persistent CTAs the tile table is dealt to
   int nreduce = 0;
   long long reduce_max = 0;       // largest M x N among them
   ugemm::SplitPlan split{};
@@ -112,8 +114,8 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
   s = split_gemm_launch(p->split, dummy, dummy, single, p->maps,
-                        static_cast<const TcProblem*>(p->probs), p->nsub, p->gemm_tiles,
-                        std::max(1, p->cfg.chunk_k / kTcKB), p->cfg.max_ctas, p->dev_err, st);
+                        static_cast<const TcProblem*>(p->probs), p->tiles, p->gemm_tiles,
+                        std::max(1, p->cfg.chunk_k / kTcKB), p->grid, p->dev_err, st);
   return s == UGEMM_OK ? reduce_launch(p, st) : s;
 }
 
@@ -445,7 +447,15 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   const size_t red_bytes = rjobs.size() * sizeof(ReduceJob);
   const size_t off_p = align_up(maps_bytes, 256), off_j = off_p + align_up(prob_bytes, 256);
   const size_t off_r = off_j + align_up(job_bytes, 256);
-  const size_t total = off_r + align_up(std::max<size_t>(red_bytes, 1), 256);
+  // split form: the tile table, dealt to exactly p->grid persistent CTAs
+  std::vector<int4> recs;
+  if (!simt) {
+    p->grid = std::max(1, std::min(tiles, p->cfg.max_ctas > 0 ? p->cfg.max_ctas : sms));
+    recs = split_tile_table(tprobs.data(), static_cast<int>(tprobs.size()), bn, p->grid);
+  }
+  const size_t rec_bytes = recs.size() * sizeof(int4);
+  const size_t off_t = off_r + align_up(std::max<size_t>(red_bytes, 1), 256);
+  const size_t total = off_t + align_up(std::max<size_t>(rec_bytes, 1), 256);
   std::vector<uint8_t> host(total, 0);
   std::memcpy(host.data(), maps.data(), maps_bytes);
   std::memcpy(host.data() + off_p, simt ? static_cast<const void*>(sprobs.data()) : tprobs.data(),
@@ -453,6 +463,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   std::memcpy(host.data() + off_j, simt ? static_cast<const void*>(pjobs.data()) : sjobs.data(),
               job_bytes);
   if (red_bytes) std::memcpy(host.data() + off_r, rjobs.data(), red_bytes);
+  if (rec_bytes) std::memcpy(host.data() + off_t, recs.data(), rec_bytes);
   e = cudaMalloc(&p->table, total);
   if (e == cudaSuccess) e = cudaMemcpy(p->table, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -464,6 +475,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   p->probs = tb + off_p;
   p->jobs = tb + off_j;
   p->reduce = tb + off_r;
+  p->tiles = reinterpret_cast<const int4*>(tb + off_t);
 
   if (flags & UGEMM_PLAN_GRAPH) {
     cudaStream_t cs;

@@ -16,9 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cstring>
-
 #include <cstddef>
+#include <cstring>
 
 #include "internal.h"
 #include "split_tc.cuh"
@@ -39,13 +38,32 @@ struct MultiTable {
 static_assert(sizeof(MultiTable) <= 4000, "multi table must fit the kernel parameter space");
 static_assert(sizeof(MultiTable) % 16 == 0, "multi table copies as 16-byte words");
 
-__global__ void multi_table_kernel(const __grid_constant__ MultiTable t, MultiTable* dst) {
-  const uint4* s = reinterpret_cast<const uint4*>(&t);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  for (int i = threadIdx.x; i < static_cast<int>(sizeof(MultiTable) / 16); i += blockDim.x)
-    d[i] = s[i];
-  // the GEMM kernel reads the tensor maps through the tensormap proxy
-  asm volatile("fence.proxy.tensormap::generic.release.gpu;" ::: "memory");
+// Block 0 copies the table; every thread also writes the tile table of a
+// grid of `grid` CTAs: CTA c takes tiles c, c + grid, c + 2 grid, ... (in
+// longest-k-first problem order), stored contiguously after the grid's
+// {first, end} ranges, one {problem, m0, n0, 0} record per tile.
+__global__ void multi_table_kernel(const __grid_constant__ MultiTable t, int nsub, int total_tiles,
+                                   int block_n, int grid, MultiTable* dst, int4* table) {
+  if (blockIdx.x == 0) {
+    const uint4* s = reinterpret_cast<const uint4*>(&t);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int i = threadIdx.x; i < static_cast<int>(sizeof(MultiTable) / 16); i += blockDim.x)
+      d[i] = s[i];
+    // the GEMM kernel reads the tensor maps through the tensormap proxy
+    asm volatile("fence.proxy.tensormap::generic.release.gpu;" ::: "memory");
+  }
+  const int per = total_tiles / grid, extra = total_tiles % grid;
+  auto first = [&](int c) { return c * per + (c < extra ? c : extra); };
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < grid; c += gridDim.x * blockDim.x)
+    table[c] = make_int4(first(c), first(c + 1), 0, 0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total_tiles; i += gridDim.x * blockDim.x) {
+    int p = 0;
+    while (p + 1 < nsub && t.probs[p + 1].tile_start <= i) ++p;
+    const TcProblem& P = t.probs[p];
+    int m0, n0;
+    tc_raster(i - P.tile_start, P.tiles_m, P.tiles_n, block_n, m0, n0);
+    table[grid + first(i % grid) + i / grid] = make_int4(p, m0, n0, 0);
+  }
 }
 
 double padded(int rows, int cols, int bn) {
@@ -65,12 +83,13 @@ struct Geo {
 };
 
 // Scratch layout: per GEMM [A pieces | B pieces], then the partial tiles of
-// the sliced GEMMs, then the table.
+// the sliced GEMMs, the table and the tile records.
 struct Layout {
   Geo geo[kMultiMax];
   int block_n = 256;
   size_t a_off[kMultiMax], b_off[kMultiMax], part_off[kMultiMax];
-  size_t table_off = 0, total = 0;
+  size_t table_off = 0, recs_off = 0, total = 0;
+  int grid = 1;  // persistent CTAs of the launch
 };
 
 Layout layout_for(const Gemm* gs, int n, const SplitPlan& p, int sms) {
@@ -122,7 +141,11 @@ Layout layout_for(const Gemm* gs, int n, const SplitPlan& p, int sms) {
     if (L.geo[i].slices > 1) off += align_up(size_t(L.geo[i].slices) * gs[i].M * gs[i].N * 4, 256);
   }
   L.table_off = align_up(off, 256);
-  L.total = L.table_off + align_up(sizeof(MultiTable), 256);
+  int tiles = 0;
+  for (int i = 0; i < n; ++i) tiles += L.geo[i].tiles * L.geo[i].slices;
+  L.grid = std::max(1, std::min(tiles, sms));
+  L.recs_off = L.table_off + align_up(sizeof(MultiTable), 256);
+  L.total = L.recs_off + align_up(size_t(L.grid + tiles) * sizeof(int4), 256);
   return L;
 }
 
@@ -202,7 +225,9 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
     tiles += t.probs[j].tiles_m * t.probs[j].tiles_n;
   }
   uint8_t* tab = base + L.table_off;
-  multi_table_kernel<<<1, 128, 0, st>>>(t, reinterpret_cast<MultiTable*>(tab));
+  int4* recs = reinterpret_cast<int4*>(base + L.recs_off);
+  multi_table_kernel<<<std::max(1, std::min(cdiv(tiles, 256), 64)), 256, 0, st>>>(
+      t, nsub, tiles, p.block_n, L.grid, reinterpret_cast<MultiTable*>(tab), recs);
   if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
@@ -210,8 +235,8 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
   ugemm_status s = split_gemm_launch(
       p, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
-      reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), nsub, tiles, chunk, 0,
-      dev_err, st);
+      reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), recs, tiles, chunk,
+      L.grid, dev_err, st);
   if (s != UGEMM_OK || nred == 0) return s;
   return splitk_reduce_launch(reinterpret_cast<const ReduceJob*>(tab + offsetof(MultiTable, red)),
                               nred, red_max, st);

@@ -44,6 +44,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <vector>
 
 #include "internal.h"
 #include "ptx.cuh"
@@ -51,8 +52,6 @@
 
 namespace ugemm {
 namespace {
-
-constexpr int kRaster = 8;
 
 // Correction products in issue order, encoded (ia << 2) | ib; the main
 // product a0*b0 is implicit.
@@ -68,30 +67,43 @@ __device__ __forceinline__ void fence_tensormap(const CUtensorMap* map) {
                : "memory");
 }
 
-// Index of the problem owning global tile t (tile_start is ascending).
-__device__ __forceinline__ int find_problem(const TcProblem* probs, int n, int t) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 struct TileCoord { int p, m0, n0; };
 
+// Tiles of this CTA: a grouped launch walks its own slice of the planned tile
+// list (tiles[blockIdx.x] = {first, end}; the records follow the grid's
+// ranges), one GEMM strides through its tiles by the grid size.
+struct TileRange { int first, end, step; };
+
+template <bool GROUPED>
+__device__ __forceinline__ TileRange tile_range(const int4* tiles, int total_tiles) {
+  if constexpr (GROUPED) {
+    const int4 r = tiles[blockIdx.x];
+    return TileRange{r.x, r.y, 1};
+  } else {
+    return TileRange{static_cast<int>(blockIdx.x), total_tiles, static_cast<int>(gridDim.x)};
+  }
+}
+
+// Tile t of one GEMM in raster order (tc_raster).  Grouped launches read the
+// same coordinates from their tile table, one 16-byte record {problem, m0,
+// n0} per tile, built when the launch is planned: a persistent CTA then pays
+// two dependent loads per tile instead of a binary search through the
+// problem records (each step an L2 round trip).
 template <int BN, bool GROUPED>
 __device__ __forceinline__ TileCoord tile_coord(const TcProblem& single, const TcProblem* probs,
-                                                int nprob, int t, TcProblem& P) {
+                                                const int4* tiles, int t, TcProblem& P) {
   TileCoord tc;
-  tc.p = GROUPED ? find_problem(probs, nprob, t) : 0;
-  P = GROUPED ? probs[tc.p] : single;
-  const int local = t - P.tile_start;
-  const int per_group = kRaster * P.tiles_n;
-  const int first_m = (local / per_group) * kRaster;
-  const int group_rows = min(P.tiles_m - first_m, kRaster);
-  tc.m0 = (first_m + (local % per_group) % group_rows) * kTcBM;
-  tc.n0 = ((local % per_group) / group_rows) * BN;
+  if constexpr (GROUPED) {
+    const int4 r = tiles[gridDim.x + t];
+    tc.p = r.x;
+    tc.m0 = r.y;
+    tc.n0 = r.z;
+    P = probs[r.x];
+  } else {
+    tc.p = 0;
+    P = single;
+    tc_raster(t - P.tile_start, P.tiles_m, P.tiles_n, BN, tc.m0, tc.n0);
+  }
   return tc;
 }
 
@@ -99,7 +111,8 @@ template <int NP, int BN, bool GROUPED, bool EPI>
 __global__ void __launch_bounds__(kTcThreads, 1)
     split_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
-                    const TcProblem* __restrict__ probs, int nprob, int total_tiles, int nprod,
+                    const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
+                    int total_tiles, int nprod,
                     int chunk_kb, int* err) {
   using S = TcShape<NP, BN>;
   extern __shared__ uint8_t smem_raw[];
@@ -146,9 +159,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       uint32_t it = 0;
       bool ok = true;
-      for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x) {
+      const TileRange tr = tile_range<GROUPED>(tiles, total_tiles);
+      for (int t = tr.first; ok && t < tr.end; t += tr.step) {
         TcProblem P;
-        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, tiles, t, P);
         const CUtensorMap* ma = GROUPED ? &maps[2 * P.map] : &tmA;
         const CUtensorMap* mb = GROUPED ? &maps[2 * P.map + 1] : &tmB;
         if (GROUPED) {
@@ -179,9 +193,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t it = 0, ntile = 0;
       uint32_t nbound[NB] = {};
       bool ok = true;
-      for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
+      const TileRange tr = tile_range<GROUPED>(tiles, total_tiles);
+      for (int t = tr.first; ok && t < tr.end; t += tr.step, ++ntile) {
         TcProblem P;
-        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, tiles, t, P);
         // a group's narrow problems and right-edge tiles multiply only the
         // columns that exist (UMMA N in steps of 16)
         uint32_t idesc = idesc_full;
@@ -245,9 +260,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t ntile = 0;
     uint32_t nbound[NB] = {};
     bool ok = true;
-    for (int t = blockIdx.x; ok && t < total_tiles; t += gridDim.x, ++ntile) {
+    const TileRange tr = tile_range<GROUPED>(tiles, total_tiles);
+    for (int t = tr.first; ok && t < tr.end; t += tr.step, ++ntile) {
       TcProblem P;
-      const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, nprob, t, P);
+      const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, tiles, t, P);
       const uint32_t buf = ntile % NB, use = ntile / NB;
       const uint32_t t_buf = tmem + buf * 2 * BN + lane_base + col_off;
       float acc[HALF];
@@ -707,7 +723,7 @@ int sm_count() {
 
 template <int NP, int BN, bool GROUPED, bool EPI>
 ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcProblem& single,
-                           const CUtensorMap* maps, const TcProblem* probs, int nprob,
+                           const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
                            int total_tiles, int nprod, int chunk_kb, int max_ctas, int* dev_err,
                            cudaStream_t st) {
   using S = TcShape<NP, BN>;
@@ -716,7 +732,7 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
   if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
   const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
-  kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, nprob, total_tiles, nprod,
+  kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, tiles, total_tiles, nprod,
                                           chunk_kb, dev_err);
   prof_end(st, GROUPED ? kProfGrouped : kProfSplitGemm);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
@@ -725,6 +741,28 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
 int kp_of(int K) { return static_cast<int>(align_up(std::max(K, 1), kTcKB)); }
 
 }  // namespace
+
+std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid) {
+  int total = 0;
+  for (int p = 0; p < nprob; ++p) total += probs[p].tiles_m * probs[p].tiles_n;
+  // CTA c takes tiles c, c + grid, c + 2 grid, ... of the longest-k-first
+  // list (measured: a longest-processing-time deal by estimated MMA work
+  // finished later, 193 vs 163 us on the 256-problem group)
+  const int per = total / grid, extra = total % grid;
+  auto first = [&](int c) { return c * per + (c < extra ? c : extra); };
+  std::vector<int4> table(grid + total);
+  for (int c = 0; c < grid; ++c) table[c] = make_int4(first(c), first(c + 1), 0, 0);
+  for (int p = 0; p < nprob; ++p) {
+    const TcProblem& P = probs[p];
+    for (int local = 0; local < P.tiles_m * P.tiles_n; ++local) {
+      const int t = P.tile_start + local;
+      int m0, n0;
+      tc_raster(local, P.tiles_m, P.tiles_n, block_n, m0, n0);
+      table[grid + first(t % grid) + t / grid] = make_int4(p, m0, n0, 0);
+    }
+  }
+  return table;
+}
 
 int split_default_chunk_kb() {
   static int chunk = 0;
@@ -814,17 +852,18 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
   const TcProblem P = split_problem(g, p.block_n, 0);
   const int total = P.tiles_m * P.tiles_n;
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
-  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, 1, total, chunk, 0, dev_err, st);
+  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr, total, chunk, 0, dev_err, st);
 }
 
 ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,
                                const TcProblem& single, const CUtensorMap* maps,
-                               const TcProblem* probs, int nprob, int total_tiles, int chunk_kb,
+                               const TcProblem* probs, const int4* tiles, int total_tiles,
+                               int chunk_kb,
                                int max_ctas, int* dev_err, cudaStream_t st) {
   const bool grouped = probs != nullptr;
 #define UGEMM_SPLIT_CASE(NP, BN, GR, EPI)                                                    \
   if (p.pieces == NP && p.block_n == BN && grouped == GR && p.epi == EPI)                   \
-    return launch_kernel<NP, BN, GR, EPI>(ta, tb, single, maps, probs, nprob, total_tiles,   \
+    return launch_kernel<NP, BN, GR, EPI>(ta, tb, single, maps, probs, tiles, total_tiles,   \
                                           p.products, chunk_kb, max_ctas, dev_err, st);
 #define UGEMM_SPLIT_CASES(NP, BN)    \
   UGEMM_SPLIT_CASE(NP, BN, false, false) \
@@ -876,7 +915,7 @@ ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void*
     return UGEMM_ERR_CUDA;
   const TcProblem P = split_problem(g, p.block_n, 0);
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
-  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, 1, P.tiles_m * P.tiles_n, chunk, 0,
+  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr, P.tiles_m * P.tiles_n, chunk, 0,
                            dev_err, st);
 }
 

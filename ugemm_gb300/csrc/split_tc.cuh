@@ -5,6 +5,8 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <vector>
+
 #include "internal.h"
 
 namespace ugemm {
@@ -13,6 +15,18 @@ constexpr int kTcBM = 128;       // rows of C per CTA tile (UMMA M)
 constexpr int kTcKB = 32;        // k depth of one pipeline stage (64-byte bf16 rows)
 constexpr int kTcEpiWarps = 8;   // two per TMEM lane quarter
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
+constexpr int kTcRaster = 8;     // tile rows per raster group (L2 reuse)
+
+// Tile `local` of a tiles_m x tiles_n GEMM: raster groups of kTcRaster tile
+// rows walked column by column, so consecutive tiles share operand rows in L2.
+__host__ __device__ __forceinline__ void tc_raster(int local, int tiles_m, int tiles_n,
+                                                   int block_n, int& m0, int& n0) {
+  const int per_group = kTcRaster * tiles_n;
+  const int first_m = (local / per_group) * kTcRaster;
+  const int group_rows = tiles_m - first_m < kTcRaster ? tiles_m - first_m : kTcRaster;
+  m0 = (first_m + (local % per_group) % group_rows) * kTcBM;
+  n0 = ((local % per_group) / group_rows) * block_n;
+}
 
 template <int NP, int BN>
 struct TcShape {
@@ -77,10 +91,17 @@ void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
                        int K, CUtensorMap* ta, CUtensorMap* tb);
 TcProblem split_problem(const Gemm& g, int block_n, int tile_start);
+// probs/tiles: a grouped launch's problem records and its tile table (from
+// split_tile_table, for a grid of exactly max_ctas CTAs); both null for one
+// GEMM (`single`).
 ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,
                                const TcProblem& single, const CUtensorMap* maps,
-                               const TcProblem* probs, int nprob, int total_tiles, int chunk_kb,
-                               int max_ctas, int* dev_err, cudaStream_t st);
+                               const TcProblem* probs, const int4* tiles, int total_tiles,
+                               int chunk_kb, int max_ctas, int* dev_err, cudaStream_t st);
+// Tile table of a grouped launch of `grid` persistent CTAs: grid ranges
+// {first, end, 0, 0} into the records that follow, one {problem, m0, n0, 0}
+// per tile (raster order within a problem), dealt round robin.
+std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid);
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st);
 ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
