@@ -83,8 +83,9 @@ def test_compat_requires_init(lib):
 
 def test_workspace_query_is_host_only(lib):
     # split-precision form: 3 bf16 pieces of A (M x Kp) and B (N x Kp)
-    n = ug.workspace_bytes("N", "N", 4096, 4096, 1024, 1024, 4096, "bf16x6")
-    assert n == 2 * 3 * 4096 * 1024 * 2
+    # (fewer tiles than SMs, shallow k: neither split-K nor a wave tail)
+    n = ug.workspace_bytes("N", "N", 1536, 1536, 512, 512, 1536, "bf16x6")
+    assert n == 2 * 3 * 1536 * 512 * 2
     # a deep k under a small output runs as split-K slices: partial tiles too
     pieces = 3 * (64 + 200) * 40000 * 2
     assert ug.workspace_bytes("N", "N", 64, 200, 40000, 40000, 200, "bf16x6") > pieces + 2 * 64 * 200 * 4

@@ -151,6 +151,87 @@ Layout layout_for(const Gemm* gs, int n, const SplitPlan& p, int sms) {
 
 }  // namespace
 
+TailPlan tail_plan(const Gemm& g, const SplitPlan& p) {
+  TailPlan t;
+  if (g.M == 0 || g.N == 0 || g.K == 0 || g.alpha == 0.f) return t;
+  const int sms = sm_count();
+  const int tiles_m = cdiv(g.M, kTcBM), tiles_n = cdiv(g.N, p.block_n);
+  const int tiles = tiles_m * tiles_n, rem = tiles % sms;
+  if (tiles <= sms || rem == 0 || split_kp(g.K) / kTcKB < 2 * kMinSlice) return t;
+  // the raster order ends with the last group of tile rows, column by column
+  const int first_m = ((tiles_m - 1) / kTcRaster) * kTcRaster, rows = tiles_m - first_m;
+  const int cols = cdiv(rem, rows);             // whole tile columns of that group
+  if (cols >= tiles_n || 2 * cols * rows > sms) return t;
+  t.use = true;
+  t.main_tiles = tiles - cols * rows;
+  t.r0 = first_m * kTcBM;
+  t.c0 = (tiles_n - cols) * p.block_n;
+  return t;
+}
+
+size_t tail_scratch_bytes(const Gemm& g, const SplitPlan& p) {
+  const TailPlan t = tail_plan(g, p);
+  if (!t.use) return 0;
+  const int tiles = 2 * cdiv(g.M - t.r0, kTcBM) * cdiv(g.N - t.c0, p.block_n);
+  return align_up(2 * size_t(g.M - t.r0) * (g.N - t.c0) * 4, 256) +
+         align_up(sizeof(MultiTable), 256) + align_up(size_t(sm_count() + tiles) * sizeof(int4), 256);
+}
+
+ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail,
+                         const void* a_pieces, const void* b_pieces, void* scratch, int* dev_err,
+                         cudaStream_t st) {
+  const int Mt = g.M - tail.r0, Nt = g.N - tail.c0, Kp = split_kp(g.K);
+  const size_t mn = size_t(Mt) * Nt;
+  uint8_t* base = static_cast<uint8_t*>(scratch);
+  float* part = reinterpret_cast<float*>(base);
+  uint8_t* tab = base + align_up(2 * mn * 4, 256);
+  int4* recs = reinterpret_cast<int4*>(tab + align_up(sizeof(MultiTable), 256));
+  MultiTable t;
+  std::memset(&t, 0, sizeof t);
+  const auto* ap = static_cast<const __nv_bfloat16*>(a_pieces) + size_t(tail.r0) * Kp;
+  const auto* bp = static_cast<const __nv_bfloat16*>(b_pieces) + size_t(tail.c0) * Kp;
+  if (!split_encode_view(p.pieces, kTcBM, ap, Mt, g.M, g.K, &t.maps[0]) ||
+      !split_encode_view(p.pieces, p.block_n, bp, Nt, g.N, g.K, &t.maps[1]))
+    return UGEMM_ERR_CUDA;
+  const int nkb = Kp / kTcKB, per = cdiv(nkb, 2);
+  int tiles = 0;
+  for (int s = 0; s < 2; ++s) {
+    TcProblem& tp = t.probs[s];
+    tp.C = part + s * mn;
+    tp.M = Mt;
+    tp.N = Nt;
+    tp.ldc = Nt;
+    tp.alpha = g.alpha;
+    tp.beta = 0.f;
+    tp.kb0 = s * per;
+    tp.nkb = std::min(per, nkb - tp.kb0);
+    tp.tiles_m = cdiv(Mt, kTcBM);
+    tp.tiles_n = cdiv(Nt, p.block_n);
+    tp.tile_start = tiles;
+    tiles += tp.tiles_m * tp.tiles_n;
+  }
+  Epilogue epi = g.epi;
+  if (epi.bias) epi.bias += tail.r0;
+  t.red[0] = ReduceJob{part, g.C + size_t(tail.r0) * g.ldc + tail.c0, Mt, Nt, g.ldc, 2, g.beta, epi};
+  const int grid = std::max(1, std::min(tiles, sm_count()));
+  multi_table_kernel<<<std::max(1, std::min(cdiv(tiles, 256), 64)), 256, 0, st>>>(
+      t, 2, tiles, p.block_n, grid, reinterpret_cast<MultiTable*>(tab), recs);
+  if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
+  SplitPlan q = p;
+  q.epi = false;
+  CUtensorMap dummy;
+  std::memset(&dummy, 0, sizeof dummy);
+  TcProblem single{};
+  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  ugemm_status s = split_gemm_launch(
+      q, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
+      reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), recs, tiles, chunk,
+      grid, dev_err, st);
+  if (s != UGEMM_OK) return s;
+  return splitk_reduce_launch(reinterpret_cast<const ReduceJob*>(tab + offsetof(MultiTable, red)),
+                              1, static_cast<long long>(mn), st);
+}
+
 bool multi_wanted(const Gemm& g, const SplitPlan& p) {
   if (g.M == 0 || g.N == 0 || g.K == 0 || g.alpha == 0.f) return false;
   const int tiles = cdiv(g.M, kTcBM) * cdiv(g.N, p.block_n);

@@ -791,7 +791,16 @@ size_t split_operand_bytes(int pieces, int rows, int K) {
 }
 
 size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p) {
-  return split_operand_bytes(p.pieces, g.M, g.K) + split_operand_bytes(p.pieces, g.N, g.K);
+  return split_operand_bytes(p.pieces, g.M, g.K) + split_operand_bytes(p.pieces, g.N, g.K) +
+         tail_scratch_bytes(g, p);
+}
+
+bool split_encode_view(int pieces, int box_rows, const void* base, int rows, int plane_rows, int K,
+                       CUtensorMap* map) {
+  const int Kp = kp_of(K);
+  const uint64_t row = uint64_t(Kp) * 2;
+  return encode_tmap_3d(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, Kp, rows, pieces, row,
+                        row * plane_rows, kTcKB, box_rows, pieces, CU_TENSOR_MAP_SWIZZLE_64B);
 }
 
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
@@ -852,7 +861,15 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
   const TcProblem P = split_problem(g, p.block_n, 0);
   const int total = P.tiles_m * P.tiles_n;
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
-  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr, total, chunk, 0, dev_err, st);
+  // a partial last wave of tiles runs as two k slices (multi.cu)
+  const TailPlan tail = tail_plan(g, p);
+  ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
+                                     tail.use ? tail.main_tiles : total, chunk, 0, dev_err, st);
+  if (s != UGEMM_OK || !tail.use) return s;
+  return tail_launch(g, p, tail, ap, bp,
+                     static_cast<uint8_t*>(ws.ptr) + split_operand_bytes(p.pieces, g.M, g.K) +
+                         split_operand_bytes(p.pieces, g.N, g.K),
+                     dev_err, st);
 }
 
 ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,

@@ -91,6 +91,25 @@ void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
                        int K, CUtensorMap* ta, CUtensorMap* tb);
 TcProblem split_problem(const Gemm& g, int block_n, int tile_start);
+// Map of rows [0, rows) of a piece array whose planes are plane_rows long
+// (a view starting inside the array: base points at its first row).
+bool split_encode_view(int pieces, int box_rows, const void* base, int rows, int plane_rows, int K,
+                       CUtensorMap* map);
+
+// Wave tail of one split GEMM (multi.cu): when the tiles' last wave would
+// occupy less than half of the SMs, its tiles -- whole tile columns of the
+// last raster group, a rectangle [r0, M) x [c0, N) of C -- run as two k
+// slices in one grouped launch plus a reduce, after the other tiles.
+struct TailPlan {
+  bool use = false;
+  int main_tiles = 0;  // tiles the single-GEMM kernel runs (raster order prefix)
+  int r0 = 0, c0 = 0;  // first row and column of the tail rectangle
+};
+TailPlan tail_plan(const Gemm& g, const SplitPlan& p);
+size_t tail_scratch_bytes(const Gemm& g, const SplitPlan& p);
+ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail,
+                         const void* a_pieces, const void* b_pieces, void* scratch, int* dev_err,
+                         cudaStream_t st);
 // probs/tiles: a grouped launch's problem records and its tile table (from
 // split_tile_table, for a grid of exactly max_ctas CTAs); both null for one
 // GEMM (`single`).
