@@ -103,3 +103,42 @@ def test_conv_stack_with_leaky_relu_forward_and_backward():
                          (st.tensor(l, "dcol", (K, N)), w_.T @ dy)):
             assert float(torch.linalg.norm(got.double() - ref) / torch.linalg.norm(ref)) < 2e-6
     st.close()
+
+
+@pytest.mark.parametrize("M,N,K", [(4096, 4096, 1024), (64, 200, 20000), (2048, 3000, 2048)])
+def test_fused_epilogue_through_split_k_and_wave_tail(M, N, K):
+    """Shapes whose split-form GEMM runs partly outside the single kernel: a
+    partial last wave run as two k slices (4096 x 4096), a deep narrow
+    problem run as split-K slices (64 x 200 x 20000): the bias (per row of C,
+    offset to the sliced rows) and the activation are applied by the reduce."""
+    g = torch.Generator(device="cuda").manual_seed(M + K)
+    W = torch.randn((M, K), device="cuda", generator=g) * (1.0 / K ** 0.5)
+    X = torch.rand((K, N), device="cuda", generator=g)
+    bias = torch.randn(M, device="cuda", generator=g)
+    C0 = torch.rand((M, N), device="cuda", generator=g)
+    Y = ug.gemm_ex(W, X, C0.clone(), bias=bias, act=1, slope=0.1, alpha=1.25, beta=0.5,
+                   precision="bf16x6")
+    torch.cuda.synchronize()
+    pre = 1.25 * (W.double() @ X.double()) + 0.5 * C0.double() + bias.double()[:, None]
+    ref = torch.where(pre > 0, pre, 0.1 * pre)
+    assert float(torch.linalg.norm(Y.double() - ref) / torch.linalg.norm(ref)) < 2e-6
+
+
+def test_grouped_split_k_problem_with_epilogue():
+    g = torch.Generator(device="cuda").manual_seed(21)
+    specs, refs = [], []
+    for (M, N, K) in [(64, 300, 30000), (200, 64, 64)]:
+        A = torch.randn((M, K), device="cuda", generator=g) * (1.0 / K ** 0.5)
+        B = torch.randn((K, N), device="cuda", generator=g)
+        C = torch.empty((M, N), device="cuda")
+        bias = torch.randn(M, device="cuda", generator=g)
+        specs.append(dict(ta="N", tb="N", M=M, N=N, K=K, alpha=1.0, beta=0.0, A=A, lda=K, B=B,
+                          ldb=N, C=C, ldc=N, bias=bias, act=1, slope=0.1))
+        pre = A.double() @ B.double() + bias.double()[:, None]
+        refs.append(torch.where(pre > 0, pre, pre * 0.1))
+    for prec in ("bf16x6", "simt"):
+        ug.sgemm_grouped(specs, precision=prec)
+        torch.cuda.synchronize()
+        for s, r in zip(specs, refs):
+            err = float(torch.linalg.norm(s["C"].double() - r) / torch.linalg.norm(r))
+            assert err < max(2e-6, 2.5e-8 * s["K"] ** 0.5), (prec, s["M"], s["K"], err)
