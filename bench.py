@@ -285,6 +285,23 @@ def profile_case(args):
     print(f"profile case {args.profile_case} size {n}: {reps} runs done")
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The slowest rank's value; every rank of the job must call it."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, seconds: float, world: int) -> float:
+    """Weak scaling: every rank processed `units_per_rank` within `seconds`
+    (the slowest rank's time), so the job's rate is world times that."""
+    return units_per_rank * world / seconds
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -373,11 +390,7 @@ def main():
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), world, torch.device("cuda", local))
         return ms / steps
 
     # --- accuracy of each form against an FP64 GEMM of the same inputs
@@ -443,10 +456,7 @@ def main():
         e2e_call()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     lib.sgemm_cuda_finish()
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world, torch.device("cuda", local))
 
     pk, pk_kind = peaks()
     tflops_split = flops / (ms_split * 1e-3) / 1e12
@@ -466,7 +476,7 @@ def main():
 
     line = {
         "metric": METRIC,
-        "value": round(tflops_split * world, 3),
+        "value": round(whole_job_rate(flops, ms_split * 1e-3, world) / 1e12, 3),
         "unit": "TFLOPS",
         "n_gpus": world,
         "steps": args.steps,
@@ -498,7 +508,7 @@ def main():
                      "kernel": "split_tc_kernel<3,256> (BF16x6)",
                      "peak_basis": f"bf16_tflops ({pk_kind} cuBLAS burst {pk['bf16_tflops']}) / 6 "
                                    "piece products; achieved = 2MNK / kernel time"},
-        "e2e": {"value": round(flops / e2e_s / 1e12 * world, 3), "unit": "TFLOPS",
+        "e2e": {"value": round(whole_job_rate(flops, e2e_s, world) / 1e12, 3), "unit": "TFLOPS",
                 "h2d_bytes_per_step": 3 * M * N * 4, "d2h_bytes_per_step": M * N * 4,
                 "api": "sgemm_cuda (compat, host pointers, pinned)"},
         "gpu_launches": int(round(launches_per_step * args.steps)),
