@@ -210,15 +210,16 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
     p->cfg = *config;
   } else {
     p->cfg = default_grouped_config(form);
-    // Untuned split plans: 256-wide tiles only pay when the problems are wide
-    // in the orientation the kernel computes them (a transposed problem's
-    // width is its M): measured, 128 wins on the 256-problem set with N in
-    // [32, 1024] and on the conv stack, whose GEMMs are 64-512 wide.
+    // Untuned split plans: 128-wide tiles only when no problem is wider than
+    // 128 columns in the orientation the kernel computes it (a transposed
+    // problem's width is its M); measured on the 256-problem set, 256-wide
+    // tiles with the staged epilogue and narrow-N MMAs win (144 vs 162 us).
     if (form != UGEMM_PREC_SIMT) {
-      double n_sum = 0;
+      int widest = 0;
       for (const Gemm& x : g)
-        n_sum += padded_area(x.N, x.M, 128) < padded_area(x.M, x.N, 128) ? x.M : x.N;
-      if (n_sum / count < 512) p->cfg.block_n = 128;
+        widest = std::max(widest,
+                          padded_area(x.N, x.M, 128) < padded_area(x.M, x.N, 128) ? x.M : x.N);
+      if (widest <= 128) p->cfg.block_n = 128;
     }
   }
   if (form != UGEMM_PREC_SIMT) {

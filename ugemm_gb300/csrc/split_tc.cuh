@@ -42,7 +42,12 @@ struct TcShape {
   // tiles have no room left and store straight from registers.
   static constexpr bool STAGE_C = (BN == 128);
   static constexpr size_t STAGE_C_BYTES = STAGE_C ? size_t(kTcEpiWarps) * 32 * 33 * 4 : 0;
-  static constexpr size_t SMEM = 1024 + size_t(STAGES) * STAGE_BYTES + 256 + STAGE_C_BYTES;
+  // 256-wide tiles of grouped launches stage 8 rows x 32 columns per warp
+  // at a time: what the stage ring leaves of shared memory
+  static constexpr bool STAGE_C8 = (BN == 256);
+  static constexpr size_t STAGE_C8_BYTES = STAGE_C8 ? size_t(kTcEpiWarps) * 8 * 33 * 4 : 0;
+  static constexpr size_t SMEM =
+      1024 + size_t(STAGES) * STAGE_BYTES + 256 + STAGE_C_BYTES + STAGE_C8_BYTES;
   // main + correction accumulators, double-buffered across tiles when they fit
   static constexpr int ACC_BUFS = (4 * BN <= 512) ? 2 : 1;
   static constexpr uint32_t TMEM_COLS = ACC_BUFS * 2 * BN;
@@ -119,7 +124,8 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                int chunk_kb, int max_ctas, int* dev_err, cudaStream_t st);
 // Tile table of a grouped launch of `grid` persistent CTAs: grid ranges
 // {first, end, 0, 0} into the records that follow, one {problem, m0, n0, 0}
-// per tile (raster order within a problem), dealt round robin.
+// per tile (raster order within a problem), dealt longest first to the
+// least-loaded CTA.
 std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid);
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st);
