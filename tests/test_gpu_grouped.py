@@ -129,13 +129,14 @@ def test_grouped_wide_and_narrow_problems(prec):
               ("T", "N", 130, 145, 77), ("N", "N", 1, 4000, 33), ("N", "T", 16, 16, 16)]
     specs, refs = make_group(shapes, seed=8, alpha=0.75, beta=-1.5, pad=5)
     keep = [s["C"][:, s["N"]:].clone() for s in specs]
-    for bn in (128, 256):
-        plan =ug.GroupedPlan(specs, precision=prec, config={"block_n": bn, "chunk_k": 256,
-                                                            "max_ctas": 0})
+    # both tile widths; a grid smaller than the GPU deals the tiles to 37 CTAs
+    for bn, ctas in ((128, 0), (256, 0), (256, 37)):
+        plan = ug.GroupedPlan(specs, precision=prec, config={"block_n": bn, "chunk_k": 256,
+                                                             "max_ctas": ctas})
         c0 = [s["C"].clone() for s in specs]
         plan.run()
         plan.check()
-        assert worst_error(specs, refs) < 2e-6, bn
+        assert worst_error(specs, refs) < 2e-6, (bn, ctas)
         for s, k in zip(specs, keep):
             assert torch.equal(s["C"][:, s["N"]:], k)
         for s, c in zip(specs, c0):  # beta != 0: restore C for the next tile width
