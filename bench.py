@@ -440,9 +440,12 @@ def main():
     hA = A.cpu().pin_memory()
     hB = B.cpu().pin_memory()
     hC = C0.cpu().pin_memory()
-    size = (M * K + K * N + M * N) * 4 + ug.workspace_bytes("N", "N", M, N, K, K, N, "bf16x6")
+    # the reference's test sizes the device buffer at ten times the three
+    # matrices (sgemm_test.c:29); the pipelined host path keeps the whole
+    # problem resident in it
+    size = (M * K + K * N + M * N) * 10 * 4
     lib = ug.load()
-    lib.sgemm_cuda_init(0, local, size + (64 << 20))
+    lib.sgemm_cuda_init(0, local, size)
     ug._check(lib.ugemm_last_error())
     lib.sgemm_cuda_set_precision(ug.PREC_BF16X6)
     e2e_steps = max(2, args.steps // 2)

@@ -1,5 +1,6 @@
 """GPU parity of the pipelined host-pointer path: large ugemm_sgemm /
-sgemm_cuda calls are cut into row bands whose copies overlap the GEMMs; the
+sgemm_cuda calls run as k slabs accumulated on the device, then row bands
+that finish the rest of k and go back while later bands compute; the
 result must equal an FP64 GEMM of the same operands, for every transpose
 pair, beta == 0 and beta != 0, padded leading dimensions, in both forms."""
 import numpy as np
@@ -61,3 +62,54 @@ def test_compat_sgemm_cuda_large_call():
     finally:
         ug.sgemm_cuda_finish()
     assert float(np.linalg.norm(C.astype(np.float64) - ref) / np.linalg.norm(ref)) < 2e-6
+
+
+def run_counted(prec, ta, tb, M, N, K, alpha, beta, seed):
+    """One host-pointer call with the launch profiler on; returns the
+    normwise error against FP64 and the pre-pass launch count."""
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(-1, 1, (M, K) if ta == "N" else (K, M)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N) if tb == "N" else (N, K)).astype(np.float32)
+    C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    ref = fp64(ta, tb, alpha, A, B, beta, C, M, N, K)
+    out = C.copy()
+    ug.profile_enable(True)
+    try:
+        ug.ugemm_sgemm("R", ta, tb, M, N, K, alpha, A, A.shape[1], B, B.shape[1], beta, out, N,
+                       precision=prec)
+        prof = ug.profile_collect()
+    finally:
+        ug.profile_enable(False)
+    err = float(np.linalg.norm(out.astype(np.float64) - ref) / np.linalg.norm(ref))
+    return err, prof["split_prepass"][1]
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "T")])
+def test_slab_then_band_schedule(ta, tb):
+    """4100 x 3000 x 2500: k1 = 1024 in one slab, the other 1476 of k in
+    five bands (1152, 1152, 1152, then the last 644 rows halved: 384 + 260):
+    the slab splits A and B, the rest of B splits once, every band splits
+    its rows."""
+    err, prep = run_counted("bf16x6", ta, tb, 4100, 3000, 2500, 1.25, 0.5, 11)
+    assert err < 2e-6, err
+    assert prep == 2 * 1 + 1 + 5
+
+
+@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+@pytest.mark.parametrize("beta", [0.0, -0.75])
+def test_bands_only_schedule_for_shallow_k(prec, beta):
+    """K < 2048: no slab phase; B whole first, then ten bands (six of 1024
+    rows, four of 512) that read their C directly (beta applied by the GEMM
+    itself)."""
+    err, prep = run_counted(prec, "N", "T", 8192, 2048, 1024, 0.5, beta, 12)
+    assert err < 2e-6, (prec, beta, err)
+    assert prep == (1 + 10 if prec == "bf16x6" else 0)
+
+
+def test_deep_k_many_slabs():
+    """K = 20000: slabs of 1280, 3840 and 4864 accumulate k1 = 9984 before
+    three bands (1024, 512, 512 rows) take the other 10016."""
+    K = 20000
+    err, prep = run_counted("bf16x6", "T", "N", 2048, 1024, K, 1.0, 0.5, 13)
+    assert err < max(2e-6, 2.5e-8 * K ** 0.5), err
+    assert prep == 2 * 3 + 1 + 3

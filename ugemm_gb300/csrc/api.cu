@@ -7,6 +7,8 @@
 // tensor-core forms, and error reporting (the reference reports none).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -389,8 +391,9 @@ int ugemm_sgemm_host(char major, char transa, char transb, int M, int N, int K, 
   // Without init: a temporary arena sized for this call.
   const int form = resolve_form(precision, g);
   const size_t a_rows = g.ta == 'N' ? g.M : g.K, b_rows = g.tb == 'N' ? g.K : g.N;
-  const size_t bytes = align_up(a_rows * g.lda * 4, 256) + align_up(b_rows * g.ldb * 4, 256) +
-                       align_up(size_t(g.M) * g.ldc * 4, 256) + scratch_for(g, form);
+  const size_t bytes = std::max(align_up(a_rows * g.lda * 4, 256) + align_up(b_rows * g.ldb * 4, 256) +
+                                    align_up(size_t(g.M) * g.ldc * 4, 256) + scratch_for(g, form),
+                                host_pipelined_bytes(g, form));
   void* arena = nullptr;
   cudaError_t e = cudaMalloc(&arena, bytes);
   if (e != cudaSuccess) return fail(UGEMM_ERR_ALLOC, "cudaMalloc(temporary arena) failed%s");

@@ -223,9 +223,12 @@ ugemm_tile_config default_grouped_config(int form);
 bool tuned_config(int count, const ugemm_problem* problems, int precision, ugemm_tile_config* cfg);
 int split_default_chunk_kb();
 
-// Host-pointer GEMM with overlapped copies (row bands of C); returns
+// Host-pointer GEMM with overlapped copies (k slabs, then row bands of C); returns
 // UGEMM_ERR_UNSUPPORTED when the call is too small or the arena too tight,
 // in which case the caller runs the plain copy-compute-copy sequence.
+// Device arena bytes the pipelined host path needs for this call (0: the
+// call is not pipelined).
+size_t host_pipelined_bytes(const Gemm& g, int form);
 ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t arena_bytes,
                                  int* dev_err, cudaStream_t caller);
 

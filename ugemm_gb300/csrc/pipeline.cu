@@ -3,23 +3,29 @@
 // The reference's sgemm_ocl (sgemm_ocl2.h:166-219) writes A, B (and C) to the
 // device, runs the kernel and reads C back, one blocking step after another,
 // and the reference's benchmarks time all of it (sgemm_test.c:229-232).
-// Here a large host-pointer GEMM is cut into blocks of C: row bands of op(A)
-// times column parts of op(B).  Every block is an independent GEMM of the
-// same operands, so the result equals the unblocked call.
-//   * copies go out, on one stream, in the order the blocks need them:
-//     band s of A, part s of B, each followed by the C blocks (when
-//     beta != 0) of the blocks it completes; so the first GEMM starts after
-//     one band of A and one part of B have crossed the host link, not after
-//     all of B, and after 2s operand copies s^2 blocks can run;
-//   * each band of A and each part of B is split into bf16 pieces once
-//     (tensor-core form) by the first block that uses it;
-//   * blocks run on two compute streams, so one block's first tiles start
-//     while the previous block's last tiles are still running, and each
-//     finished block of C goes back on its own stream while later blocks
-//     compute.
-// Device staging: all bands of A and parts of B (and their pieces), four
-// block slots of C, all with 16-byte pitches so that TMA can describe them
-// whatever the host leading dimensions are.
+// Here a large host-pointer GEMM runs in two phases whose copies, GEMMs and
+// copies back overlap:
+//   1. k slabs.  op(A)[:, k0:k0+w] and op(B)[k0:k0+w, :] cross the host link
+//      slab by slab; each slab is a rank-w update of a device accumulator
+//      (the first with beta = 0, so C is not needed yet).  Per byte copied a
+//      slab carries 2MN/(4(M+N)) flops, more than the GEMMs can retire at
+//      the link's rate, so the GEMMs run back to back from the first slab on.
+//   2. row bands.  The rest of op(B) (k >= k1) crosses once; then, band by
+//      band, the rest of op(A)'s rows and the band of C.  A band's C is
+//      folded into the accumulator (acc += beta * C, an axpy), the band's
+//      last GEMM (k >= k1, with the bias / activation epilogue) finishes it,
+//      and it goes back to the host while later bands compute -- so the
+//      copy back of C overlaps the copies in, instead of following the last
+//      GEMM.
+// Phase 1 alone would finish every row of C at the very end (each needs all
+// of k); phase 2 alone would keep the GEMMs idle until all of op(B) is in.
+// With k1 about half of K both the link and the tensor cores stay busy.
+// The result is the same GEMM with the k sum cut at slab boundaries (one
+// FP32 add per boundary and element).
+// Device staging: op(A), op(B), C and (beta != 0) the incoming C, whole, with
+// 16-byte pitches so that TMA can describe them whatever the host leading
+// dimensions are; in the split forms each slab and band is split into bf16
+// pieces once, on its own stream, while the previous GEMM runs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,16 +38,17 @@
 namespace ugemm {
 namespace {
 
-constexpr int kMaxBands = 8, kMaxParts = 8, kMaxBlocks = kMaxBands * kMaxParts;
-constexpr int kCSlots = 4;
+constexpr int kMaxSlabs = 16, kMaxBands = 64;
 
 struct PipeState {
   bool ready = false;
-  cudaStream_t h2d = nullptr, d2h = nullptr, comp[2] = {nullptr, nullptr};
-  // per band: A copied, A split, all blocks computed; per part: B copied, B
-  // split; per block: C copied, computed, copied back; plus one entry event
-  cudaEvent_t a_in[kMaxBands], a_split[kMaxBands], b_in[kMaxParts], b_split[kMaxParts];
-  cudaEvent_t c_in[kMaxBlocks], comp_done[kMaxBlocks], c_out[kMaxBlocks], entry;
+  // h2d: every copy in, in the order the GEMMs need it; prep: splits and
+  // the beta * C folds; gemm[0]: the slab GEMMs, then even bands; gemm[1]:
+  // odd bands; d2h: finished bands back
+  cudaStream_t h2d = nullptr, d2h = nullptr, prep = nullptr, gemm[2] = {nullptr, nullptr};
+  cudaEvent_t entry, acc_done, rest_in, rest_ready, last_out;
+  cudaEvent_t slab_in[kMaxSlabs], slab_ready[kMaxSlabs];
+  cudaEvent_t band_in[kMaxBands], band_ready[kMaxBands], band_done[kMaxBands];
 };
 
 std::mutex g_pmu;
@@ -53,18 +60,21 @@ ugemm_status pipe_state(PipeState** out) {
   PipeState& p = g_pipe[dev];
   if (!p.ready) {
     const unsigned fl = cudaStreamNonBlocking;
-    if (cudaStreamCreateWithFlags(&p.h2d, fl) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&p.d2h, fl) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&p.comp[0], fl) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&p.comp[1], fl) != cudaSuccess)
+    // the splits and folds run at the highest priority: their CTAs do not fit
+    // beside a running GEMM's, so they go first whenever one ends
+    int lo = 0, hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&p.prep, fl, hi) != cudaSuccess)
       return UGEMM_ERR_CUDA;
-    std::vector<cudaEvent_t*> all = {&p.entry};
-    for (int i = 0; i < kMaxBands; ++i) { all.push_back(&p.a_in[i]); all.push_back(&p.a_split[i]); }
-    for (int j = 0; j < kMaxParts; ++j) { all.push_back(&p.b_in[j]); all.push_back(&p.b_split[j]); }
-    for (int b = 0; b < kMaxBlocks; ++b) {
-      all.push_back(&p.c_in[b]);
-      all.push_back(&p.comp_done[b]);
-      all.push_back(&p.c_out[b]);
+    for (cudaStream_t* s : {&p.h2d, &p.d2h, &p.gemm[0], &p.gemm[1]})
+      if (cudaStreamCreateWithFlags(s, fl) != cudaSuccess) return UGEMM_ERR_CUDA;
+    std::vector<cudaEvent_t*> all = {&p.entry, &p.acc_done, &p.rest_in, &p.rest_ready,
+                                     &p.last_out};
+    for (int i = 0; i < kMaxSlabs; ++i) { all.push_back(&p.slab_in[i]); all.push_back(&p.slab_ready[i]); }
+    for (int r = 0; r < kMaxBands; ++r) {
+      all.push_back(&p.band_in[r]);
+      all.push_back(&p.band_ready[r]);
+      all.push_back(&p.band_done[r]);
     }
     for (cudaEvent_t* e : all)
       if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return UGEMM_ERR_CUDA;
@@ -80,40 +90,139 @@ bool is_split(int form) {
 
 int pitch4(int n) { return static_cast<int>(align_up(n, 4)); }
 
+// Layout of one pipelined call: k1 = depth of the slab phase (0: bands
+// only), the slab width and band height, the device pitches and the bytes of
+// every staging buffer.
+struct Layout {
+  bool split = false, fold = false;
+  int k1 = 0, k2 = 0, nslab = 0, nband = 0;
+  std::vector<int> slab_k0, slab_w;  // slab i: k in [slab_k0[i], slab_k0[i] + slab_w[i])
+  std::vector<int> band_m0, band_h;  // band r: rows [band_m0[r], band_m0[r] + band_h[r])
+  int lda_d = 0, ldb_d = 0, ldc_d = 0;
+  long long a_sr = 0, a_sk = 0, b_sr = 0, b_sk = 0;
+  SplitPlan plan, plan_acc;
+  size_t a_bytes = 0, b_bytes = 0, c_bytes = 0, tail_acc = 0, tail_band = 0, band_ap = 0,
+         rest_bp = 0, total = 0;
+  std::vector<size_t> slab_ap, slab_bp;
+};
+
+// The slab GEMMs: no epilogue, it belongs to each band's last GEMM.
+Gemm acc_gemm(const Gemm& g) {
+  Gemm a = g;
+  a.epi = Epilogue{};
+  return a;
+}
+
+bool pipe_layout(const Gemm& g, int form, Layout* out) {
+  Layout L;
+  L.split = is_split(form);
+  if (!L.split && form != UGEMM_PREC_SIMT) return false;
+  if (g.K == 0 || g.alpha == 0.f || g.M < 2048) return false;
+  const size_t bytes = 4 * (size_t(g.M) * g.K + size_t(g.K) * g.N + size_t(g.M) * g.N);
+  if (bytes < (size_t(64) << 20)) return false;
+  // bands of whole 128-row tiles, about 1024 rows each, the last quarter of
+  // them halved: the last band's GEMM and copy back are what is left after
+  // the last byte has crossed the link
+  const int nb0 = std::min(std::max(g.M / 1024, 2), kMaxBands / 2);
+  const int band = static_cast<int>(align_up(cdiv(g.M, nb0), 128));
+  const int halved = cdiv(nb0, 4);
+  for (int m0 = 0, r = 0; m0 < g.M; m0 += band, ++r) {
+    const int h = std::min(band, g.M - m0);
+    const int h0 = static_cast<int>(align_up(cdiv(h, 2), 128));
+    if (r >= nb0 - halved && h0 < h) {
+      L.band_h.push_back(h0);
+      L.band_h.push_back(h - h0);
+    } else {
+      L.band_h.push_back(h);
+    }
+  }
+  // slab phase: half of k, when k is deep enough for it to pay, in slabs of
+  // an eighth, three eighths and a half of it: the first GEMM starts after
+  // a small slab has crossed, and each slab's copy hides behind the
+  // previous slab's GEMM
+  if (g.K >= 2048) {
+    const int k1 = g.K / 2 / 256 * 256;
+    const int w0 = static_cast<int>(align_up(k1 / 8, 256)), w1 = static_cast<int>(align_up(3 * k1 / 8, 256));
+    if (k1 >= 2048 && w0 + w1 < k1) {
+      L.slab_w = {w0, w1, k1 - w0 - w1};
+    } else {
+      L.slab_w = {k1};
+    }
+  }
+  L.k1 = 0;
+  for (int w : L.slab_w) { L.slab_k0.push_back(L.k1); L.k1 += w; }
+  for (int m0 = 0, r = 0; r < static_cast<int>(L.band_h.size()); m0 += L.band_h[r++]) L.band_m0.push_back(m0);
+  L.nslab = static_cast<int>(L.slab_w.size());
+  L.nband = static_cast<int>(L.band_h.size());
+  L.ldc_d = pitch4(g.N);
+  if (L.nband < 2 || L.nband > kMaxBands || L.nslab > kMaxSlabs || L.k1 >= g.K) return false;
+  int rows = 0;
+  for (int h : L.band_h) {
+    if (h <= 0 || size_t(h) * L.ldc_d >= (size_t(1) << 31)) return false;
+    rows += h;
+  }
+  for (int w : L.slab_w)
+    if (w <= 0) return false;
+  if (rows != g.M) return false;
+  L.k2 = g.K - L.k1;
+  L.fold = g.beta != 0.f && L.k1 > 0;
+  // device layouts: op(A) and op(B) in their host storage order, whole
+  const int a_rows = g.ta == 'N' ? g.M : g.K, a_cols = g.ta == 'N' ? g.K : g.M;
+  const int b_rows = g.tb == 'N' ? g.K : g.N, b_cols = g.tb == 'N' ? g.N : g.K;
+  L.lda_d = pitch4(a_cols);
+  L.ldb_d = pitch4(b_cols);
+  // op(A)(m, k) at dA[m*a_sr + k*a_sk]; op(B)^T(n, k) at dB[n*b_sr + k*b_sk]
+  L.a_sr = g.ta == 'N' ? L.lda_d : 1;
+  L.a_sk = g.ta == 'N' ? 1 : L.lda_d;
+  L.b_sr = g.tb == 'N' ? 1 : L.ldb_d;
+  L.b_sk = g.tb == 'N' ? L.ldb_d : 1;
+  L.a_bytes = align_up(size_t(a_rows) * L.lda_d * 4, 256);
+  L.b_bytes = align_up(size_t(b_rows) * L.ldb_d * 4, 256);
+  L.c_bytes = align_up(size_t(g.M) * L.ldc_d * 4, 256);
+  L.slab_ap.assign(L.nslab, 0);
+  L.slab_bp.assign(L.nslab, 0);
+  if (L.split) {
+    const Gemm ga = acc_gemm(g);
+    L.plan = split_plan_for(form, g);
+    L.plan_acc = split_plan_for(form, ga);
+    for (int i = 0; i < L.nslab; ++i) {
+      Gemm gs = ga;
+      gs.K = L.slab_w[i];
+      L.slab_ap[i] = split_operand_bytes(L.plan.pieces, g.M, gs.K);
+      L.slab_bp[i] = split_operand_bytes(L.plan.pieces, g.N, gs.K);
+      L.tail_acc = std::max(L.tail_acc, tail_scratch_bytes(gs, L.plan_acc));
+    }
+    for (int h : L.band_h) L.band_ap = std::max(L.band_ap, split_operand_bytes(L.plan.pieces, h, L.k2));
+    L.rest_bp = split_operand_bytes(L.plan.pieces, g.N, L.k2);
+    for (int mb : L.band_h) {
+      Gemm gb = g;
+      gb.M = mb;
+      gb.K = L.k2;
+      L.tail_band = std::max(L.tail_band, tail_scratch_bytes(gb, L.plan));
+    }
+  }
+  L.total = L.a_bytes + L.b_bytes + L.c_bytes * (L.fold ? 2 : 1) + L.tail_acc + 2 * L.tail_band +
+            size_t(L.nband) * L.band_ap + L.rest_bp;
+  for (int i = 0; i < L.nslab; ++i) L.total += L.slab_ap[i] + L.slab_bp[i];
+  *out = std::move(L);
+  return true;
+}
+
 }  // namespace
+
+size_t host_pipelined_bytes(const Gemm& g, int form) {
+  Layout L;
+  return pipe_layout(g, form, &L) ? L.total : 0;
+}
 
 ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t arena_bytes,
                                  int* dev_err, cudaStream_t caller) {
-  const bool split = is_split(form);
-  if (!split && form != UGEMM_PREC_SIMT) return UGEMM_ERR_UNSUPPORTED;
-  if (g.K == 0 || g.alpha == 0.f || g.M < 1024) return UGEMM_ERR_UNSUPPORTED;
-  const size_t a_rows = g.ta == 'N' ? g.M : g.K, a_cols = g.ta == 'N' ? g.K : g.M;
-  const size_t b_rows = g.tb == 'N' ? g.K : g.N, b_cols = g.tb == 'N' ? g.N : g.K;
-  const size_t bytes = 4 * (a_rows * a_cols + b_rows * b_cols + size_t(g.M) * g.N);
-  if (bytes < (size_t(64) << 20)) return UGEMM_ERR_UNSUPPORTED;
-
-  // blocks: about four bands of whole 128-row tiles times about four parts
-  // of whole 256-column tiles
-  int band = static_cast<int>(align_up(std::max(512, cdiv(g.M, 4)), 128));
-  while (cdiv(g.M, band) > kMaxBands) band += 128;
-  int part = static_cast<int>(align_up(std::max(1024, cdiv(g.N, 4)), 256));
-  while (cdiv(g.N, part) > kMaxParts) part += 256;
-  const int nb = cdiv(g.M, band), npart = cdiv(g.N, part);
-  if (nb < 2) return UGEMM_ERR_UNSUPPORTED;
-
-  SplitPlan plan{};
-  if (split) plan = split_plan_for(form, g);
-  // device pitches (floats) and slot sizes
-  const int lda_d = g.ta == 'N' ? pitch4(g.K) : pitch4(band);   // band: band x K or K x band
-  const int ldb_d = g.tb == 'N' ? pitch4(part) : pitch4(g.K);   // part: K x part or part x K
-  const int ldc_d = pitch4(part);
-  const size_t a_slot = align_up(size_t(g.ta == 'N' ? band : g.K) * lda_d * 4, 256);
-  const size_t b_slot = align_up(size_t(g.tb == 'N' ? g.K : part) * ldb_d * 4, 256);
-  const size_t c_slot = align_up(size_t(band) * ldc_d * 4, 256);
-  const size_t ap_slot = split ? split_operand_bytes(plan.pieces, band, g.K) : 0;
-  const size_t bp_slot = split ? split_operand_bytes(plan.pieces, part, g.K) : 0;
-  const size_t need = npart * (b_slot + bp_slot) + nb * (a_slot + ap_slot) + kCSlots * c_slot;
-  if (need > arena_bytes) return UGEMM_ERR_UNSUPPORTED;
+  Layout L;
+  if (!pipe_layout(g, form, &L) || L.total > arena_bytes) return UGEMM_ERR_UNSUPPORTED;
+  const bool split = L.split, fold = L.fold;
+  const int k1 = L.k1, k2 = L.k2, lda_d = L.lda_d, ldb_d = L.ldb_d, ldc_d = L.ldc_d;
+  const long long a_sr = L.a_sr, a_sk = L.a_sk, b_sr = L.b_sr, b_sk = L.b_sk;
+  const Gemm g_acc = acc_gemm(g);
 
   std::lock_guard<std::mutex> lock(g_pmu);
   PipeState* ps = nullptr;
@@ -121,131 +230,143 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   uint8_t* base = static_cast<uint8_t*>(arena);
   size_t off = 0;
   auto take = [&](size_t n) { uint8_t* p = base + off; off += n; return p; };
-  float* dB[kMaxParts];
-  void* dBp[kMaxParts] = {};
-  for (int j = 0; j < npart; ++j) {
-    dB[j] = reinterpret_cast<float*>(take(b_slot));
-    if (split) dBp[j] = take(bp_slot);
+  float* dA = reinterpret_cast<float*>(take(L.a_bytes));
+  float* dB = reinterpret_cast<float*>(take(L.b_bytes));
+  float* dC = reinterpret_cast<float*>(take(L.c_bytes));
+  float* dCin = fold ? reinterpret_cast<float*>(take(L.c_bytes)) : dC;
+  void* tail_s_acc = L.tail_acc ? take(L.tail_acc) : nullptr;
+  void* tail_s_band[2] = {L.tail_band ? take(L.tail_band) : nullptr,
+                          L.tail_band ? take(L.tail_band) : nullptr};
+  std::vector<void*> sap(L.nslab), sbp(L.nslab), bap(L.nband);
+  void* rbp = nullptr;
+  if (split) {
+    for (int i = 0; i < L.nslab; ++i) { sap[i] = take(L.slab_ap[i]); sbp[i] = take(L.slab_bp[i]); }
+    for (int r = 0; r < L.nband; ++r) bap[r] = take(L.band_ap);
+    rbp = take(L.rest_bp);
   }
-  float* dA[kMaxBands];
-  void* dAp[kMaxBands] = {};
-  for (int s = 0; s < nb; ++s) {
-    dA[s] = reinterpret_cast<float*>(take(a_slot));
-    if (split) dAp[s] = take(ap_slot);
-  }
-  float* dC[kCSlots];
-  for (int s = 0; s < kCSlots; ++s) dC[s] = reinterpret_cast<float*>(take(c_slot));
   auto ck = [](cudaError_t e) { return e == cudaSuccess; };
+
+  // a region of op(A) (rows m0.., k0..) or op(B) (k0.., columns n0..) from
+  // the host operand into the same place of the device copy
+  auto copy_a = [&](int m0, int mr, int k0, int kw) {
+    const int r0 = g.ta == 'N' ? m0 : k0, c0 = g.ta == 'N' ? k0 : m0;
+    const int nr = g.ta == 'N' ? mr : kw, nc = g.ta == 'N' ? kw : mr;
+    return ck(cudaMemcpy2DAsync(dA + size_t(r0) * lda_d + c0, size_t(lda_d) * 4,
+                                g.A + size_t(r0) * g.lda + c0, size_t(g.lda) * 4, size_t(nc) * 4,
+                                nr, cudaMemcpyHostToDevice, ps->h2d));
+  };
+  auto copy_b = [&](int k0, int kw) {  // all N columns of op(B), k rows k0..k0+kw
+    const int r0 = g.tb == 'N' ? k0 : 0, c0 = g.tb == 'N' ? 0 : k0;
+    const int nr = g.tb == 'N' ? kw : g.N, nc = g.tb == 'N' ? g.N : kw;
+    return ck(cudaMemcpy2DAsync(dB + size_t(r0) * ldb_d + c0, size_t(ldb_d) * 4,
+                                g.B + size_t(r0) * g.ldb + c0, size_t(g.ldb) * 4, size_t(nc) * 4,
+                                nr, cudaMemcpyHostToDevice, ps->h2d));
+  };
+  auto a_view = [&](int m0, int k0) { return dA + m0 * a_sr + k0 * a_sk; };
+  auto b_view = [&](int k0) { return dB + k0 * b_sk; };
 
   // work queued earlier on the caller's stream comes first
   if (!ck(cudaEventRecord(ps->entry, caller))) return UGEMM_ERR_CUDA;
-  for (cudaStream_t s : {ps->h2d, ps->d2h, ps->comp[0], ps->comp[1]})
+  for (cudaStream_t s : {ps->h2d, ps->d2h, ps->prep, ps->gemm[0], ps->gemm[1]})
     if (!ck(cudaStreamWaitEvent(s, ps->entry, 0))) return UGEMM_ERR_CUDA;
 
-  bool a_split_done[kMaxBands] = {}, b_split_done[kMaxParts] = {};
-  auto copy_a = [&](int i) {
-    const int m0 = i * band, mb = std::min(band, g.M - m0);
-    bool ok;
-    if (g.ta == 'N')  // rows m0 .. m0+mb of the M x K operand
-      ok = ck(cudaMemcpy2DAsync(dA[i], size_t(lda_d) * 4, g.A + size_t(m0) * g.lda,
-                                size_t(g.lda) * 4, size_t(g.K) * 4, mb, cudaMemcpyHostToDevice,
-                                ps->h2d));
-    else              // columns m0 .. m0+mb of the K x M operand
-      ok = ck(cudaMemcpy2DAsync(dA[i], size_t(lda_d) * 4, g.A + m0, size_t(g.lda) * 4,
-                                size_t(mb) * 4, g.K, cudaMemcpyHostToDevice, ps->h2d));
-    return ok && ck(cudaEventRecord(ps->a_in[i], ps->h2d));
-  };
-  auto copy_b = [&](int j) {
-    const int n0 = j * part, nw = std::min(part, g.N - n0);
-    bool ok;
-    if (g.tb == 'N')  // columns n0 .. n0+nw of the K x N operand
-      ok = ck(cudaMemcpy2DAsync(dB[j], size_t(ldb_d) * 4, g.B + n0, size_t(g.ldb) * 4,
-                                size_t(nw) * 4, g.K, cudaMemcpyHostToDevice, ps->h2d));
-    else              // rows n0 .. n0+nw of the N x K operand
-      ok = ck(cudaMemcpy2DAsync(dB[j], size_t(ldb_d) * 4, g.B + size_t(n0) * g.ldb,
-                                size_t(g.ldb) * 4, size_t(g.K) * 4, nw, cudaMemcpyHostToDevice,
-                                ps->h2d));
-    return ok && ck(cudaEventRecord(ps->b_in[j], ps->h2d));
-  };
-  int blk = 0;
-  auto run_block = [&](int i, int j) -> ugemm_status {
-    const int m0 = i * band, mb = std::min(band, g.M - m0);
-    const int n0 = j * part, nw = std::min(part, g.N - n0), cs_slot = blk % kCSlots;
-    cudaStream_t cs = ps->comp[blk & 1];
-    // block (i, j) of C into its slot once the slot's previous block is home
-    if (blk >= kCSlots) cudaStreamWaitEvent(ps->h2d, ps->c_out[blk - kCSlots], 0);
-    if (g.beta != 0.f &&  // beta == 0: C is not read (sgemm_ocl2.h:177)
-        !ck(cudaMemcpy2DAsync(dC[cs_slot], size_t(ldc_d) * 4, g.C + size_t(m0) * g.ldc + n0,
-                              size_t(g.ldc) * 4, size_t(nw) * 4, mb, cudaMemcpyHostToDevice,
-                              ps->h2d)))
+  // ---- copies in, in the order the GEMMs consume them
+  for (int i = 0; i < L.nslab; ++i) {
+    const int k0 = L.slab_k0[i], w = L.slab_w[i];
+    if (!copy_a(0, g.M, k0, w) || !copy_b(k0, w) || !ck(cudaEventRecord(ps->slab_in[i], ps->h2d)))
       return UGEMM_ERR_CUDA;
-    if (!ck(cudaEventRecord(ps->c_in[blk], ps->h2d))) return UGEMM_ERR_CUDA;
-    // operands: the band's and the part's pieces, split by their first user
-    if (!a_split_done[i]) {
-      cudaStreamWaitEvent(cs, ps->a_in[i], 0);
-      if (split) {
-        const long long sr = g.ta == 'N' ? lda_d : 1, sk = g.ta == 'N' ? 1 : lda_d;
-        if (split_operand_launch(plan.pieces, dA[i], sr, sk, mb, g.K, dAp[i], cs) != UGEMM_OK)
-          return UGEMM_ERR_CUDA;
-      }
-      cudaEventRecord(ps->a_split[i], cs);
-      a_split_done[i] = true;
+  }
+  if (!copy_b(k1, k2) || !ck(cudaEventRecord(ps->rest_in, ps->h2d))) return UGEMM_ERR_CUDA;
+  for (int r = 0; r < L.nband; ++r) {
+    const int m0 = L.band_m0[r], mb = L.band_h[r];
+    if (!copy_a(m0, mb, k1, k2)) return UGEMM_ERR_CUDA;
+    if (g.beta != 0.f &&  // beta == 0: C is not read (sgemm_ocl2.h:177)
+        !ck(cudaMemcpy2DAsync(dCin + size_t(m0) * ldc_d, size_t(ldc_d) * 4,
+                              g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, size_t(g.N) * 4, mb,
+                              cudaMemcpyHostToDevice, ps->h2d)))
+      return UGEMM_ERR_CUDA;
+    if (!ck(cudaEventRecord(ps->band_in[r], ps->h2d))) return UGEMM_ERR_CUDA;
+  }
+
+  // ---- phase 1: slab GEMMs into the accumulator dC, one after another
+  cudaStream_t g0 = ps->gemm[0];
+  for (int i = 0; i < L.nslab; ++i) {
+    const int k0 = L.slab_k0[i], w = L.slab_w[i];
+    if (split) {
+      cudaStreamWaitEvent(ps->prep, ps->slab_in[i], 0);
+      if (split_operand_launch(L.plan.pieces, a_view(0, k0), a_sr, a_sk, g.M, w, sap[i], ps->prep) !=
+              UGEMM_OK ||
+          split_operand_launch(L.plan.pieces, b_view(k0), b_sr, b_sk, g.N, w, sbp[i], ps->prep) !=
+              UGEMM_OK)
+        return UGEMM_ERR_CUDA;
+      if (!ck(cudaEventRecord(ps->slab_ready[i], ps->prep))) return UGEMM_ERR_CUDA;
+      cudaStreamWaitEvent(g0, ps->slab_ready[i], 0);
     } else {
-      cudaStreamWaitEvent(cs, ps->a_split[i], 0);
+      cudaStreamWaitEvent(g0, ps->slab_in[i], 0);
     }
-    if (!b_split_done[j]) {
-      cudaStreamWaitEvent(cs, ps->b_in[j], 0);
-      if (split) {
-        const long long sr = g.tb == 'N' ? 1 : ldb_d, sk = g.tb == 'N' ? ldb_d : 1;
-        if (split_operand_launch(plan.pieces, dB[j], sr, sk, nw, g.K, dBp[j], cs) != UGEMM_OK)
-          return UGEMM_ERR_CUDA;
-      }
-      cudaEventRecord(ps->b_split[j], cs);
-      b_split_done[j] = true;
-    } else {
-      cudaStreamWaitEvent(cs, ps->b_split[j], 0);
+    Gemm gs = g_acc;
+    gs.K = w;
+    gs.A = a_view(0, k0);
+    gs.lda = lda_d;
+    gs.B = b_view(k0);
+    gs.ldb = ldb_d;
+    gs.C = dC;
+    gs.ldc = ldc_d;
+    gs.beta = i == 0 ? 0.f : 1.f;
+    ugemm_status st = split ? split_gemm_on_pieces(gs, L.plan_acc, sap[i], sbp[i], tail_s_acc, dev_err, g0)
+                            : simt_launch(gs, simt_pick_tile(gs), Scratch{nullptr, 0}, dev_err, g0);
+    if (st != UGEMM_OK) return st;
+  }
+  if (!ck(cudaEventRecord(ps->acc_done, g0))) return UGEMM_ERR_CUDA;
+
+  // ---- phase 2: the rest of op(B), then band by band
+  cudaStreamWaitEvent(ps->prep, ps->rest_in, 0);
+  if (split && split_operand_launch(L.plan.pieces, b_view(k1), b_sr, b_sk, g.N, k2, rbp,
+                                    ps->prep) != UGEMM_OK)
+    return UGEMM_ERR_CUDA;
+  if (!ck(cudaEventRecord(ps->rest_ready, ps->prep))) return UGEMM_ERR_CUDA;
+  for (int r = 0; r < L.nband; ++r) {
+    const int m0 = L.band_m0[r], mb = L.band_h[r];
+    cudaStream_t gs_st = ps->gemm[r & 1];
+    cudaStreamWaitEvent(ps->prep, ps->band_in[r], 0);
+    if (split && split_operand_launch(L.plan.pieces, a_view(m0, k1), a_sr, a_sk, mb, k2, bap[r],
+                                      ps->prep) != UGEMM_OK)
+      return UGEMM_ERR_CUDA;
+    if (fold) {  // acc += beta * C, once the slab GEMMs are done with acc
+      if (r == 0) cudaStreamWaitEvent(ps->prep, ps->acc_done, 0);
+      const int st = ugemm_saxpy(mb * ldc_d, g.beta, dCin + size_t(m0) * ldc_d, 1,
+                                 dC + size_t(m0) * ldc_d, 1, ps->prep);
+      if (st != UGEMM_OK) return UGEMM_ERR_CUDA;
     }
-    cudaStreamWaitEvent(cs, ps->c_in[blk], 0);
+    if (!ck(cudaEventRecord(ps->band_ready[r], ps->prep))) return UGEMM_ERR_CUDA;
+    cudaStreamWaitEvent(gs_st, ps->band_ready[r], 0);
+    cudaStreamWaitEvent(gs_st, ps->rest_ready, 0);
+    cudaStreamWaitEvent(gs_st, ps->acc_done, 0);
     Gemm gb = g;
     gb.M = mb;
-    gb.N = nw;
-    gb.A = dA[i];
+    gb.K = k2;
+    gb.A = a_view(m0, k1);
     gb.lda = lda_d;
-    gb.B = dB[j];
+    gb.B = b_view(k1);
     gb.ldb = ldb_d;
-    gb.C = dC[cs_slot];
+    gb.C = dC + size_t(m0) * ldc_d;
     gb.ldc = ldc_d;
+    if (k1 > 0) gb.beta = 1.f;       // acc (with beta * C folded in)
     if (gb.epi.bias) gb.epi.bias += m0;  // per-row bias follows the band
-    ugemm_status st;
-    if (split) st = split_gemm_on_pieces(gb, plan, dAp[i], dBp[j], dev_err, cs);
-    else st = simt_launch(gb, simt_pick_tile(gb), Scratch{nullptr, 0}, dev_err, cs);
-    if (st != UGEMM_OK || !ck(cudaEventRecord(ps->comp_done[blk], cs))) return UGEMM_ERR_CUDA;
-    cudaStreamWaitEvent(ps->d2h, ps->comp_done[blk], 0);
-    if (!ck(cudaMemcpy2DAsync(g.C + size_t(m0) * g.ldc + n0, size_t(g.ldc) * 4, dC[cs_slot],
-                              size_t(ldc_d) * 4, size_t(nw) * 4, mb, cudaMemcpyDeviceToHost,
-                              ps->d2h)) ||
-        !ck(cudaEventRecord(ps->c_out[blk], ps->d2h)))
+    ugemm_status st = split ? split_gemm_on_pieces(gb, L.plan, bap[r], rbp, tail_s_band[r & 1],
+                                                   dev_err, gs_st)
+                            : simt_launch(gb, simt_pick_tile(gb), Scratch{nullptr, 0}, dev_err,
+                                          gs_st);
+    if (st != UGEMM_OK || !ck(cudaEventRecord(ps->band_done[r], gs_st))) return UGEMM_ERR_CUDA;
+    cudaStreamWaitEvent(ps->d2h, ps->band_done[r], 0);
+    if (!ck(cudaMemcpy2DAsync(g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, dC + size_t(m0) * ldc_d,
+                              size_t(ldc_d) * 4, size_t(g.N) * 4, mb, cudaMemcpyDeviceToHost,
+                              ps->d2h)))
       return UGEMM_ERR_CUDA;
-    ++blk;
-    return UGEMM_OK;
-  };
-  // shells: band s of A, the blocks it completes with the parts already in,
-  // then part s of B and the blocks it completes -- after 2s copies of
-  // operands, s^2 blocks can run
-  for (int s = 0; s < std::max(nb, npart); ++s) {
-    if (s < nb) {
-      if (!copy_a(s)) return UGEMM_ERR_CUDA;
-      for (int j = 0; j < std::min(s, npart); ++j)
-        if (run_block(s, j) != UGEMM_OK) return UGEMM_ERR_CUDA;
-    }
-    if (s < npart) {
-      if (!copy_b(s)) return UGEMM_ERR_CUDA;
-      for (int i = 0; i <= std::min(s, nb - 1); ++i)
-        if (run_block(i, s) != UGEMM_OK) return UGEMM_ERR_CUDA;
-    }
   }
   // the caller's stream resumes after the last copy back
-  cudaStreamWaitEvent(caller, ps->c_out[blk - 1], 0);
+  if (!ck(cudaEventRecord(ps->last_out, ps->d2h))) return UGEMM_ERR_CUDA;
+  cudaStreamWaitEvent(caller, ps->last_out, 0);
   return cudaStreamSynchronize(ps->d2h) == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
 

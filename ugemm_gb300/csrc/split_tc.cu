@@ -981,14 +981,19 @@ ugemm_status split_operand_launch(int pieces, const float* src, long long sr, lo
 
 // GEMM on pieces already split: C = alpha * A*B^T-pieces + beta * C.
 ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
-                                  const void* b_pieces, int* dev_err, cudaStream_t st) {
+                                  const void* b_pieces, void* tail_scratch, int* dev_err,
+                                  cudaStream_t st) {
   CUtensorMap ta, tb;
   if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb))
     return UGEMM_ERR_CUDA;
   const TcProblem P = split_problem(g, p.block_n, 0);
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
-  return split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr, P.tiles_m * P.tiles_n, chunk, 0,
-                           dev_err, st);
+  const TailPlan tail = tail_scratch ? tail_plan(g, p) : TailPlan{};
+  ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
+                                     tail.use ? tail.main_tiles : P.tiles_m * P.tiles_n, chunk, 0,
+                                     dev_err, st);
+  if (s != UGEMM_OK || !tail.use) return s;
+  return tail_launch(g, p, tail, a_pieces, b_pieces, tail_scratch, dev_err, st);
 }
 
 }  // namespace ugemm

@@ -131,7 +131,10 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
                                   cudaStream_t st);
 ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
                                   int rows, int K, void* dst, cudaStream_t st);
+// GEMM on operands already split; with tail_scratch (tail_scratch_bytes of
+// it), a short last wave of tiles runs as the wave-tail launch.
 ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
-                                  const void* b_pieces, int* dev_err, cudaStream_t st);
+                                  const void* b_pieces, void* tail_scratch, int* dev_err,
+                                  cudaStream_t st);
 
 }  // namespace ugemm
