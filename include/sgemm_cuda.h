@@ -51,6 +51,8 @@ typedef enum {
   UGEMM_PREC_BF16X6 = 2, /* 3 bf16 pieces per operand, 6 piece products (tcgen05) */
   UGEMM_PREC_BF16X9 = 3, /* 3 bf16 pieces per operand, all 9 piece products (tcgen05) */
   UGEMM_PREC_BF16X3 = 4, /* 2 bf16 pieces, 3 products: ~16-bit accuracy, for error studies */
+  UGEMM_PREC_FP16X3 = 5, /* 2 fp16 pieces of the operand scaled by a power of two, 3 products
+                            (tcgen05): 22-bit operands, half the MMAs of BF16X6 */
 } ugemm_precision;
 
 /* ------------------------------------------------------------------ */

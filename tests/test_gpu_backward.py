@@ -78,7 +78,7 @@ def run_backward(ta, tb, M, N, K, alpha, prec, seed, beta_acc=0.0):
     return A, B, W, dA0, dB0, dA, dB
 
 
-@pytest.mark.parametrize("prec", ["simt", "bf16x6"])
+@pytest.mark.parametrize("prec", ["simt", "bf16x6", "fp16x3"])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
 def test_backward_small_vs_fp64(prec, ta, tb):
     M, N, K = 150, 97, 203
@@ -95,7 +95,7 @@ def test_backward_small_vs_fp64(prec, ta, tb):
 
 
 @pytest.mark.parametrize("shape", [(4096, 4096, 4096), (2048, 8192, 1024)])
-@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "simt"])
 def test_backward_config3_fd_and_cpu_gradient(shape, prec):
     """North-star config 3: loss sum(W*C), A,B ~ U[-1,1), W ~ N(0,1), NN."""
     M, N, K = shape

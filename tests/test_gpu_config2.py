@@ -2,8 +2,8 @@
 at 8192^3 and the ragged 4095 x 4097 x 1023, alpha = 1.5, beta = 0.5, all
 four transpose pairs, on U[-1,1) inputs and on a wide-range set (mantissa
 U[1,2), random sign, exponent uniform in [-8, 8]); normwise error of both
-forms against an FP64 GEMM on the GPU.  The split form must be at least as
-accurate as the FP32 SIMT form on every case."""
+forms against an FP64 GEMM on the GPU.  Both split forms (BF16x6 and FP16x3)
+must be at least as accurate as the FP32 SIMT form on every case."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -38,7 +38,7 @@ def errors(ta, tb, M, N, K, kind, seed):
     ref = ALPHA * ((A.double() if ta == "N" else A.double().T) @
                    (B.double() if tb == "N" else B.double().T)) + BETA * C0.double()
     out = {}
-    for prec in ("simt", "bf16x6"):
+    for prec in ("simt", "bf16x6", "fp16x3"):
         C = C0.clone()
         ug.sgemm_dev(ta, tb, M, N, K, ALPHA, A, A.stride(0), B, B.stride(0), BETA, C, N,
                      precision=prec)
@@ -53,6 +53,8 @@ def errors(ta, tb, M, N, K, kind, seed):
 def test_split_at_least_as_accurate_as_simt(shape, ta, tb, kind):
     M, N, K = shape
     e = errors(ta, tb, M, N, K, kind, seed=M + 2 * N + 3 * K + ord(ta) + 5 * ord(tb))
-    print(f"{shape} {ta}{tb} {kind}: simt {e['simt']:.3e} bf16x6 {e['bf16x6']:.3e}")
+    print(f"{shape} {ta}{tb} {kind}: simt {e['simt']:.3e} bf16x6 {e['bf16x6']:.3e} "
+          f"fp16x3 {e['fp16x3']:.3e}")
     assert e["bf16x6"] <= e["simt"], e
+    assert e["fp16x3"] <= e["simt"], e
     assert e["simt"] < 1e-5

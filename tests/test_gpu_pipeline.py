@@ -29,7 +29,7 @@ def fp64(ta, tb, alpha, A, B, beta, C, M, N, K):
     return (alpha * (a @ b) + beta * c).cpu().numpy()
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "simt"])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
 @pytest.mark.parametrize("beta", [0.0, 0.5])
 def test_banded_host_gemm_matches_fp64(prec, ta, tb, beta):

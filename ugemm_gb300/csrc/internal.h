@@ -146,6 +146,7 @@ struct SplitPlan {
   int products;      // number of piece products accumulated (3, 6 or 9)
   int block_n;       // CTA tile width (128 or 256)
   int chunk_kb = 0;  // k-blocks per main-accumulator chunk (0: library default)
+  bool f16 = false;  // FP16x3: scaled fp16 pieces (pieces == 2) instead of bf16
   bool epi = false;  // some problem carries a bias or activation: launch the
                      // kernel instantiation that has the fused epilogue
 };

@@ -208,6 +208,10 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
     tp.tiles_m = cdiv(Mt, kTcBM);
     tp.tiles_n = cdiv(Nt, p.block_n);
     tp.tile_start = tiles;
+    if (p.f16) {  // the views share the whole operands' scales
+      tp.fmax_a = split_fmax_word(a_pieces, p.pieces, g.M, g.K);
+      tp.fmax_b = split_fmax_word(b_pieces, p.pieces, g.N, g.K);
+    }
     tiles += tp.tiles_m * tp.tiles_n;
   }
   Epilogue epi = g.epi;
@@ -266,8 +270,8 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
     void* bp = base + L.b_off[i];
     long long a_sr, a_sk, b_sr, b_sk;
     split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
-    ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st);
-    if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st);
+    ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st, p.f16);
+    if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st, p.f16);
     if (s != UGEMM_OK) return s;
     const bool ok = o.swap ? split_encode_maps(p.pieces, p.block_n, bp, g.N, ap, g.M, g.K,
                                                &t.maps[2 * i], &t.maps[2 * i + 1])
@@ -292,6 +296,12 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
       tp.map = i;
       tp.epi = sliced ? Epilogue{} : g.epi;
       p.epi |= tp.epi.bias != nullptr || tp.epi.act != 0;
+      if (p.f16) {  // kernel operand a is op(B)^T's pieces when swapped
+        unsigned* wa = split_fmax_word(ap, p.pieces, g.M, g.K);
+        unsigned* wb = split_fmax_word(bp, p.pieces, g.N, g.K);
+        tp.fmax_a = o.swap ? wb : wa;
+        tp.fmax_b = o.swap ? wa : wb;
+      }
     }
     if (sliced) {
       t.red[nred++] = ReduceJob{part, g.C, g.M, g.N, g.ldc, o.slices, g.beta, g.epi};

@@ -85,7 +85,8 @@ ugemm_status pipe_state(PipeState** out) {
 }
 
 bool is_split(int form) {
-  return form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9 || form == UGEMM_PREC_BF16X3;
+  return form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9 || form == UGEMM_PREC_BF16X3 ||
+         form == UGEMM_PREC_FP16X3;
 }
 
 int pitch4(int n) { return static_cast<int>(align_up(n, 4)); }
@@ -294,10 +295,10 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
     const int k0 = L.slab_k0[i], w = L.slab_w[i];
     if (split) {
       cudaStreamWaitEvent(ps->prep, ps->slab_in[i], 0);
-      if (split_operand_launch(L.plan.pieces, a_view(0, k0), a_sr, a_sk, g.M, w, sap[i], ps->prep) !=
-              UGEMM_OK ||
-          split_operand_launch(L.plan.pieces, b_view(k0), b_sr, b_sk, g.N, w, sbp[i], ps->prep) !=
-              UGEMM_OK)
+      if (split_operand_launch(L.plan.pieces, a_view(0, k0), a_sr, a_sk, g.M, w, sap[i], ps->prep,
+                               L.plan.f16) != UGEMM_OK ||
+          split_operand_launch(L.plan.pieces, b_view(k0), b_sr, b_sk, g.N, w, sbp[i], ps->prep,
+                               L.plan.f16) != UGEMM_OK)
         return UGEMM_ERR_CUDA;
       if (!ck(cudaEventRecord(ps->slab_ready[i], ps->prep))) return UGEMM_ERR_CUDA;
       cudaStreamWaitEvent(g0, ps->slab_ready[i], 0);
@@ -322,7 +323,7 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   // ---- phase 2: the rest of op(B), then band by band
   cudaStreamWaitEvent(ps->prep, ps->rest_in, 0);
   if (split && split_operand_launch(L.plan.pieces, b_view(k1), b_sr, b_sk, g.N, k2, rbp,
-                                    ps->prep) != UGEMM_OK)
+                                    ps->prep, L.plan.f16) != UGEMM_OK)
     return UGEMM_ERR_CUDA;
   if (!ck(cudaEventRecord(ps->rest_ready, ps->prep))) return UGEMM_ERR_CUDA;
   for (int r = 0; r < L.nband; ++r) {
@@ -330,7 +331,7 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
     cudaStream_t gs_st = ps->gemm[r & 1];
     cudaStreamWaitEvent(ps->prep, ps->band_in[r], 0);
     if (split && split_operand_launch(L.plan.pieces, a_view(m0, k1), a_sr, a_sk, mb, k2, bap[r],
-                                      ps->prep) != UGEMM_OK)
+                                      ps->prep, L.plan.f16) != UGEMM_OK)
       return UGEMM_ERR_CUDA;
     if (fold) {  // acc += beta * C, once the slab GEMMs are done with acc
       if (r == 0) cudaStreamWaitEvent(ps->prep, ps->acc_done, 0);

@@ -40,6 +40,7 @@
 // All mbarrier waits are bounded (ptx.cuh); on a timeout the kernel records
 // an error, abandons its remaining work and still frees its TMEM.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
                     const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                     int total_tiles, int nprod,
-                    int chunk_kb, int* err) {
+                    int chunk_kb, int f16, int* err) {
   using S = TcShape<NP, BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -191,7 +192,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      constexpr uint32_t idesc_full = umma_idesc(1, 1, kTcBM, BN);
+      // operand format: bf16 pieces (1) or the FP16x3 form's fp16 pieces (0)
+      const uint32_t fmt = (NP == 2 && f16) ? 0u : 1u;
+      const uint32_t idesc_full = umma_idesc(fmt, fmt, kTcBM, BN);
       const uint32_t base = smem_u32(smem);
       uint32_t it = 0, ntile = 0;
       uint32_t nbound[NB] = {};
@@ -205,7 +208,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         uint32_t idesc = idesc_full;
         if constexpr (GROUPED) {
           const int n_rem = P.N - tc.n0;
-          if (n_rem < BN) idesc = umma_idesc(1, 1, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
+          if (n_rem < BN) idesc = umma_idesc(fmt, fmt, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
         }
         const uint32_t buf = ntile % NB, use = ntile / NB;
         const uint32_t t_main = tmem + buf * 2 * BN, t_corr = t_main + BN;
@@ -316,6 +319,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmem_empty[buf]);
+      if constexpr (NP == 2) {  // FP16x3: undo the operands' power-of-two scales
+        if (P.fmax_a != nullptr) {
+          float s1, s2;
+          f16_unscale(*P.fmax_a, *P.fmax_b, s1, s2);
+#pragma unroll
+          for (int j = 0; j < HALF; ++j) acc[j] = acc[j] * s1 * s2;
+        }
+      }
       // alpha/beta epilogue (C not read when beta == 0).  The bias /
       // activation exists only in the EPI instantiation, so the plain kernel's
       // epilogue carries no code for it.
@@ -456,16 +467,50 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // ---------------------------------------------------------------- split pass
+// Pieces of two consecutive k of one row, each piece plane as one packed
+// 16-bit pair: bf16 pieces (x0 = bf16(x), x1 = bf16(x - x0), ...) or, with
+// F16, the FP16x3 form's two fp16 pieces of x * sc (sc = 2^e from
+// f16_scale_exp; only two-piece operands use it).
+template <int NP, bool F16>
+__device__ __forceinline__ void pieces_pair(float x0, float x1, float sc, uint32_t (&out)[NP]) {
+  if constexpr (F16) {
+    const float y0 = x0 * sc, y1 = x1 * sc;
+    const __half h00 = __float2half_rn(y0), h01 = __float2half_rn(y1);
+    const __half2 hi = __halves2half2(h00, h01);
+    const __half2 lo = __halves2half2(__float2half_rn(y0 - __half2float(h00)),
+                                      __float2half_rn(y1 - __half2float(h01)));
+    out[0] = *reinterpret_cast<const uint32_t*>(&hi);
+    out[1] = *reinterpret_cast<const uint32_t*>(&lo);
+    return;
+  }
+  float rem[2] = {x0, x1};
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const __nv_bfloat16 a = __float2bfloat16_rn(rem[0]), b = __float2bfloat16_rn(rem[1]);
+    rem[0] -= __bfloat162float(a);
+    rem[1] -= __bfloat162float(b);
+    __nv_bfloat162 two;
+    two.x = a;
+    two.y = b;
+    out[p] = *reinterpret_cast<const uint32_t*>(&two);
+  }
+}
+
+// Scale of an operand's FP16x3 pieces (1 for bf16 pieces).
+__device__ __forceinline__ float f16_scale_of(const unsigned* fmax) {
+  return fmax ? pow2f(f16_scale_exp(*fmax)) : 1.f;
+}
+
 // One 32-row x 64-k tile of op(X) (element (r, k) at src[r*sr + k*sk]) into
 // NP bf16 planes dst[p][rows][Kp], through shared memory so that both source
 // layouts are read coalesced: float4 loads along the contiguous dimension
 // when the operand allows it, one 16-byte store of 8 k per plane per thread.
 // Zero for k >= K.
-template <int NP>
+template <int NP, bool F16>
 __device__ __forceinline__ void split_tile(const float* __restrict__ src, long long sr,
                                            long long sk, int rows, int K, int Kp,
                                            __nv_bfloat16* __restrict__ dst, int r0, int k0,
-                                           float (*tile)[65]) {
+                                           float (*tile)[65], const unsigned* fmax) {
   const int t = threadIdx.x;
   const bool kcontig = sk == 1;
   const long long other = kcontig ? sr : sk;
@@ -508,26 +553,14 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ src, long l
   const int r = r0 + rr, k = k0 + g8;
   if (r < rows && k < Kp) {
     const size_t plane = static_cast<size_t>(rows) * Kp;
-    uint32_t packed[3][4];
+    const float sc = F16 ? f16_scale_of(fmax) : 1.f;
+    uint32_t packed[NP][4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
-      __nv_bfloat16 pc[3][2];
+      uint32_t two[NP];
+      pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], sc, two);
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        float rem = tile[rr][g8 + e + h];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          pc[p][h] = __float2bfloat16_rn(rem);
-          rem = rem - __bfloat162float(pc[p][h]);
-        }
-      }
-#pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        __nv_bfloat162 two;
-        two.x = pc[p][0];
-        two.y = pc[p][1];
-        packed[p][e / 2] = *reinterpret_cast<uint32_t*>(&two);
-      }
+      for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
     }
     const size_t off = static_cast<size_t>(r) * Kp + k;
 #pragma unroll
@@ -537,13 +570,60 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ src, long l
   }
 }
 
-template <int NP>
+template <int NP, bool F16>
 __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restrict__ src,
                                                            long long sr, long long sk, int rows,
                                                            int K, int Kp,
-                                                           __nv_bfloat16* __restrict__ dst) {
+                                                           __nv_bfloat16* __restrict__ dst,
+                                                           const unsigned* fmax) {
   __shared__ float tile[32][65];
-  split_tile<NP>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile);
+  split_tile<NP, F16>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile, fmax);
+}
+
+// Largest magnitude of an operand stored as R rows x Cc columns with leading
+// dimension ld (the maximum does not depend on which of them is k), folded
+// into *word with atomicMax on its IEEE pattern, which orders non-negative
+// floats like their values.  NaNs are skipped (fmaxf); an infinity makes the
+// FP16x3 scale 1.  Blocks walk (row, 4096-column chunk) items grid-stride and
+// fold once at the end.
+__global__ void __launch_bounds__(256) operand_max_kernel(const float* __restrict__ src,
+                                                          long long ld, int R, int Cc,
+                                                          unsigned* word) {
+  const int chunks = (Cc + 4095) / 4096;
+  const long long items = static_cast<long long>(R) * chunks;
+  const bool vec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) && ((ld & 3) == 0);
+  float m = 0.f;
+  for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+    const long long r = it / chunks;
+    const int c0 = static_cast<int>(it - r * chunks) * 4096;
+    const int cend = min(Cc, c0 + 4096);
+    const float* row = src + r * ld;
+    if (vec) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int c = c0 + i * 1024 + threadIdx.x * 4;
+        if (c + 3 < cend) {
+          const float4 v = *reinterpret_cast<const float4*>(row + c);
+          m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+        } else {
+          for (int e = 0; e < 4; ++e)
+            if (c + e < cend) m = fmaxf(m, fabsf(row[c + e]));
+        }
+      }
+    } else {
+      for (int c = c0 + threadIdx.x; c < cend; c += 256) m = fmaxf(m, fabsf(row[c]));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float warp_max[8];
+  if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = warp_max[0];
+    for (int w = 1; w < 8; ++w) b = fmaxf(b, warp_max[w]);
+    if (b > 0.f) atomicMax(word, __float_as_uint(b));
+  }
 }
 
 // Raw values of one 32 x 64 tile, read with the same float4 pattern as
@@ -646,33 +726,21 @@ __device__ __forceinline__ void raw_to_smem(const SplitJob& j, const RawTile& in
 
 // bf16 pieces of one tile from shared memory: 8 consecutive k of one row per
 // thread, one 16-byte store per plane.
-template <int NP>
+template <int NP, bool F16>
 __device__ __forceinline__ void split_store(const SplitJob& j, int r0, int k0, float (*tile)[65]) {
   const int t = threadIdx.x;
   const int rr = t >> 3, g8 = (t & 7) * 8;
   const int r = r0 + rr, k = k0 + g8;
   if (r >= j.rows || k >= j.Kp) return;
   const size_t plane = static_cast<size_t>(j.rows) * j.Kp;
-  uint32_t packed[3][4];
+  const float sc = F16 ? f16_scale_of(j.fmax) : 1.f;
+  uint32_t packed[NP][4];
 #pragma unroll
   for (int e = 0; e < 8; e += 2) {
-    __nv_bfloat16 pc[3][2];
+    uint32_t two[NP];
+    pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], sc, two);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      float rem = tile[rr][g8 + e + h];
-#pragma unroll
-      for (int p = 0; p < NP; ++p) {
-        pc[p][h] = __float2bfloat16_rn(rem);
-        rem = rem - __bfloat162float(pc[p][h]);
-      }
-    }
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      __nv_bfloat162 two;
-      two.x = pc[p][0];
-      two.y = pc[p][1];
-      packed[p][e / 2] = *reinterpret_cast<uint32_t*>(&two);
-    }
+    for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
   }
   const size_t off = static_cast<size_t>(r) * j.Kp + k;
 #pragma unroll
@@ -730,7 +798,7 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
       load_raw(nxt, nr0, nk0, raw);
     }
     __syncthreads();
-    split_store<NP>(cur, r0, k0, tile);
+    split_store<NP, false>(cur, r0, k0, tile);
     __syncthreads();
     cur = nxt;
     r0 = nr0;
@@ -740,10 +808,17 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
 
 template <int NP>
 void launch_split(const float* src, long long sr, long long sk, int rows, int K, int Kp,
-                  __nv_bfloat16* dst, cudaStream_t st) {
+                  __nv_bfloat16* dst, cudaStream_t st, const unsigned* fmax = nullptr) {
   dim3 grid(cdiv(Kp, 64), cdiv(rows, 32));
   prof_begin(st);
-  split_pieces_kernel<NP><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, Kp, dst);
+  if constexpr (NP == 2) {  // the FP16x3 form has two pieces
+    if (fmax) {
+      split_pieces_kernel<2, true><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, Kp, dst, fmax);
+      prof_end(st, kProfSplitPrep);
+      return;
+    }
+  }
+  split_pieces_kernel<NP, false><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, Kp, dst, nullptr);
   prof_end(st, kProfSplitPrep);
 }
 
@@ -761,8 +836,8 @@ int sm_count() {
 template <int NP, int BN, bool GROUPED, bool EPI>
 ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcProblem& single,
                            const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
-                           int total_tiles, int nprod, int chunk_kb, int max_ctas, int* dev_err,
-                           cudaStream_t st) {
+                           int total_tiles, int nprod, int chunk_kb, int max_ctas, bool f16,
+                           int* dev_err, cudaStream_t st) {
   using S = TcShape<NP, BN>;
   auto kern = split_tc_kernel<NP, BN, GROUPED, EPI>;
   static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
@@ -770,7 +845,7 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
   const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
   kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, tiles, total_tiles, nprod,
-                                          chunk_kb, dev_err);
+                                          chunk_kb, f16 ? 1 : 0, dev_err);
   prof_end(st, GROUPED ? kProfGrouped : kProfSplitGemm);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
@@ -834,6 +909,7 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
   switch (precision) {
     case UGEMM_PREC_BF16X9: p.pieces = 3; p.products = 9; break;
     case UGEMM_PREC_BF16X3: p.pieces = 2; p.products = 3; break;
+    case UGEMM_PREC_FP16X3: p.pieces = 2; p.products = 3; p.f16 = true; break;
     default: p.pieces = 3; p.products = 6; break;
   }
   p.block_n = (g.N > 128) ? 256 : 128;
@@ -842,7 +918,12 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
 }
 
 size_t split_operand_bytes(int pieces, int rows, int K) {
-  return align_up(size_t(pieces) * rows * kp_of(K) * 2, 256);
+  return align_up(size_t(pieces) * rows * kp_of(K) * 2, 256) + (pieces == 2 ? 256 : 0);
+}
+
+unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K) {
+  return reinterpret_cast<unsigned*>(const_cast<uint8_t*>(static_cast<const uint8_t*>(pieces_base)) +
+                                     align_up(size_t(pieces) * rows * kp_of(K) * 2, 256));
 }
 
 size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p) {
@@ -903,7 +984,11 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
                                                split_operand_bytes(p.pieces, g.M, g.K));
   long long a_sr, a_sk, b_sr, b_sk;
   split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
-  if (p.pieces == 3) {
+  if (p.f16) {
+    ugemm_status s = split_operand_launch(2, g.A, a_sr, a_sk, g.M, g.K, ap, st, true);
+    if (s == UGEMM_OK) s = split_operand_launch(2, g.B, b_sr, b_sk, g.N, g.K, bp, st, true);
+    if (s != UGEMM_OK) return s;
+  } else if (p.pieces == 3) {
     launch_split<3>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
     launch_split<3>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
   } else {
@@ -913,7 +998,11 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
   CUtensorMap ta, tb;
   if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb))
     return UGEMM_ERR_CUDA;
-  const TcProblem P = split_problem(g, p.block_n, 0);
+  TcProblem P = split_problem(g, p.block_n, 0);
+  if (p.f16) {
+    P.fmax_a = split_fmax_word(ap, 2, g.M, g.K);
+    P.fmax_b = split_fmax_word(bp, 2, g.N, g.K);
+  }
   const int total = P.tiles_m * P.tiles_n;
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
   // a partial last wave of tiles runs as two k slices (multi.cu)
@@ -936,7 +1025,7 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
 #define UGEMM_SPLIT_CASE(NP, BN, GR, EPI)                                                    \
   if (p.pieces == NP && p.block_n == BN && grouped == GR && p.epi == EPI)                   \
     return launch_kernel<NP, BN, GR, EPI>(ta, tb, single, maps, probs, tiles, total_tiles,   \
-                                          p.products, chunk_kb, max_ctas, dev_err, st);
+                                          p.products, chunk_kb, max_ctas, p.f16, dev_err, st);
 #define UGEMM_SPLIT_CASES(NP, BN)    \
   UGEMM_SPLIT_CASE(NP, BN, false, false) \
   UGEMM_SPLIT_CASE(NP, BN, false, true)  \
@@ -971,11 +1060,30 @@ namespace ugemm {
 // Split one operand (element (r, k) at src[r*sr + k*sk]) into `pieces` bf16
 // planes [pieces][rows][Kp] at dst.
 ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
-                                  int rows, int K, void* dst, cudaStream_t st) {
+                                  int rows, int K, void* dst, cudaStream_t st, bool f16) {
   const int Kp = kp_of(K);
   auto* d = static_cast<__nv_bfloat16*>(dst);
-  if (pieces == 3) launch_split<3>(src, sr, sk, rows, K, Kp, d, st);
-  else launch_split<2>(src, sr, sk, rows, K, Kp, d, st);
+  if (f16) {
+    if (pieces != 2) return UGEMM_ERR_ARG;
+    unsigned* word = split_fmax_word(dst, 2, rows, K);
+    if (cudaMemsetAsync(word, 0, sizeof(unsigned), st) != cudaSuccess) return UGEMM_ERR_CUDA;
+    if (rows > 0 && K > 0) {
+      // the stored matrix: rows x K (k contiguous) or K x rows
+      const bool kcontig = sk == 1;
+      const int R = kcontig ? rows : K, Cc = kcontig ? K : rows;
+      const long long ld = kcontig ? sr : sk;
+      const long long items = static_cast<long long>(R) * ((Cc + 4095) / 4096);
+      const int grid = static_cast<int>(std::min<long long>(items, sm_count() * 8LL));
+      prof_begin(st);
+      operand_max_kernel<<<grid, 256, 0, st>>>(src, ld, R, Cc, word);
+      prof_end(st, kProfSplitPrep);
+    }
+    launch_split<2>(src, sr, sk, rows, K, Kp, d, st, word);
+  } else if (pieces == 3) {
+    launch_split<3>(src, sr, sk, rows, K, Kp, d, st);
+  } else {
+    launch_split<2>(src, sr, sk, rows, K, Kp, d, st);
+  }
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
 
@@ -986,7 +1094,11 @@ ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void*
   CUtensorMap ta, tb;
   if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb))
     return UGEMM_ERR_CUDA;
-  const TcProblem P = split_problem(g, p.block_n, 0);
+  TcProblem P = split_problem(g, p.block_n, 0);
+  if (p.f16) {
+    P.fmax_a = split_fmax_word(a_pieces, 2, g.M, g.K);
+    P.fmax_b = split_fmax_word(b_pieces, 2, g.N, g.K);
+  }
   const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
   const TailPlan tail = tail_scratch ? tail_plan(g, p) : TailPlan{};
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,

@@ -17,6 +17,37 @@ constexpr int kTcEpiWarps = 8;   // two per TMEM lane quarter
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
 constexpr int kTcRaster = 8;     // tile rows per raster group (L2 reuse)
 
+// FP16x3 form: each FP32 operand is scaled by a power of two 2^e, chosen from
+// its largest magnitude m so that m * 2^e lies in [2^14, 2^15), and written
+// as two fp16 pieces h0 = fp16(x 2^e), h1 = fp16(x 2^e - h0) (11 + 11
+// significand bits; the rest, < 2^-22 |x| 2^e, is dropped with the h1*g1
+// product).  The scale keeps fp16 from overflowing (largest 65504) and keeps
+// both pieces of the large elements normal (h1 >= 2^-14), so the products
+// carry 22 bits of every element that matters in the normwise sense.  `bits`
+// is the IEEE pattern of m; the exponent is clamped so that 2^e and 2^-e are
+// normal floats (all-zero or non-finite operands get e = 0).
+__host__ __device__ __forceinline__ int f16_scale_exp(unsigned bits) {
+  if (bits == 0u || bits >= 0x7F800000u) return 0;
+  const int biased = static_cast<int>(bits >> 23);
+  const int e = 14 - (biased == 0 ? -127 : biased - 127);
+  return e < -113 ? -113 : (e > 126 ? 126 : e);
+}
+// 2^e for -126 <= e <= 127, exactly.
+__host__ __device__ __forceinline__ float pow2f(int e) {
+  union { unsigned u; float f; } v;
+  v.u = static_cast<unsigned>(127 + e) << 23;
+  return v.f;
+}
+// Factors s1 * s2 = 2^-(eA + eB) that undo both operands' scales, each a
+// normal float, applied one after the other so that the intermediate stays
+// between the accumulator's and the result's magnitudes.
+__host__ __device__ __forceinline__ void f16_unscale(unsigned a_bits, unsigned b_bits, float& s1,
+                                                     float& s2) {
+  const int e = f16_scale_exp(a_bits) + f16_scale_exp(b_bits), e1 = e / 2;
+  s1 = pow2f(-e1);
+  s2 = pow2f(-(e - e1));
+}
+
 // Tile `local` of a tiles_m x tiles_n GEMM: raster groups of kTcRaster tile
 // rows walked column by column, so consecutive tiles share operand rows in L2.
 __host__ __device__ __forceinline__ void tc_raster(int local, int tiles_m, int tiles_n,
@@ -73,6 +104,10 @@ struct TcProblem {
   int swap = 0;
   int map = 0;          // tensor maps of this problem: maps[2 * map], maps[2 * map + 1]
   Epilogue epi;
+  // FP16x3 form: the largest magnitudes of the kernel's a and b operands
+  // (f16_scale_exp); the epilogue undoes their scales.  Null otherwise.
+  const unsigned* fmax_a = nullptr;
+  const unsigned* fmax_b = nullptr;
 };
 
 // One operand to split in the batched pre-pass.
@@ -86,11 +121,18 @@ struct SplitJob {
   // 2 = rows are taps and k pixels; 0 = plain strided matrix
   int gather = 0;
   Im2col im;
+  // FP16x3 form: the operand's largest magnitude (operand_max_launch), from
+  // which the pieces' power-of-two scale follows; null: bf16 pieces.
+  const unsigned* fmax = nullptr;
 };
 
 int split_kp(int K);
 int split_default_chunk_kb();
+// Bytes of one operand's pieces [pieces][rows][Kp]; two-piece operands also
+// carry a 256-byte trailer whose first word is the operand's largest
+// magnitude (split_fmax_word), used by the FP16x3 form.
 size_t split_operand_bytes(int pieces, int rows, int K);
+unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K);
 void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
                            long long* b_sk);
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
@@ -129,8 +171,11 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
 std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid);
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st);
+// Split one operand into its pieces at dst (split_operand_bytes of room).
+// f16: FP16x3 pieces -- the largest magnitude is first found into the
+// operand's trailer word (cleared here), then the pieces are scaled by it.
 ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
-                                  int rows, int K, void* dst, cudaStream_t st);
+                                  int rows, int K, void* dst, cudaStream_t st, bool f16 = false);
 // GEMM on operands already split; with tail_scratch (tail_scratch_bytes of
 // it), a short last wave of tiles runs as the wave-tail launch.
 ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
