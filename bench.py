@@ -145,7 +145,7 @@ def grouped_forms(ug, torch, stream, steps):
         refs.append(((A.double() if ta == "N" else A.double().T) @
                      (B.double() if tb == "N" else B.double().T)))
     out = {"problems": len(shapes), "flops": sum(2.0 * m * n * k for _, _, m, n, k in shapes)}
-    for prec in ("bf16x6", "simt"):
+    for prec in ("bf16x6", "fp16x3", "simt"):
         cfg, _ = ug.tune_grouped(specs, precision=prec)
         plan = ug.GroupedPlan(specs, precision=prec, config=cfg, graph=True)
         for _ in range(3):
@@ -164,9 +164,11 @@ def grouped_forms(ug, torch, stream, steps):
         ms = e0.elapsed_time(e1) / reps
         out[prec] = {"tflops": round(out["flops"] / (ms * 1e-3) / 1e12, 3), "ms": round(ms, 4),
                      "max_normwise_err_fp64": err, "config": plan.config,
-                     "launches_per_run": 2}
+                     "launches_per_run": 3 if prec == "fp16x3" else 2}
         plan.close()
-    out["split_over_simt"] = round(out["bf16x6"]["tflops"] / out["simt"]["tflops"], 3)
+    best = max(("bf16x6", "fp16x3"), key=lambda p: out[p]["tflops"])
+    out["split_over_simt"] = round(out[best]["tflops"] / out["simt"]["tflops"], 3)
+    out["best_split"] = best
     return out
 
 
@@ -212,8 +214,8 @@ def conv_forms(ug, torch, stream, steps):
     batch = 32
     layers = workloads.conv_layers(batch)
     out = {"layers": len(layers), "batch": batch, "im2col": "implicit (gathered in the operand pass)"}
-    for name, prec, explicit in (("bf16x6", "bf16x6", False), ("simt", "simt", False),
-                                 ("bf16x6_explicit_im2col", "bf16x6", True)):
+    for name, prec, explicit in (("bf16x6", "bf16x6", False), ("fp16x3", "fp16x3", False),
+                                 ("simt", "simt", False), ("bf16x6_explicit_im2col", "bf16x6", True)):
         st = ug.ConvStack(layers, batch, precision=prec, graph=True, im2col=explicit)
         g = torch.Generator(device="cuda").manual_seed(SEED + 5)
         cin, _, h, w, _ = layers[0]

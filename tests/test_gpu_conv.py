@@ -110,7 +110,8 @@ def layer_col(stack, layers, batch, l, explicit):
     return col
 
 
-@pytest.mark.parametrize("prec,explicit", [("bf16x6", False), ("simt", False), ("bf16x6", True)])
+@pytest.mark.parametrize("prec,explicit", [("bf16x6", False), ("fp16x3", False), ("simt", False),
+                                           ("bf16x6", True)])
 def test_config5_conv_stack_per_layer_fp64(prec, explicit):
     batch = 32
     layers = workloads.conv_layers(batch)
@@ -165,7 +166,7 @@ def test_conv_stack_graph_replay_is_deterministic():
     stack.close()
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "simt"])
 def test_implicit_im2col_equals_explicit(prec):
     """Gathering col inside the operand pass reads exactly the values the
     im2col pass would have stored: every Y and the top layer's dW are

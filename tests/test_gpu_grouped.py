@@ -47,7 +47,7 @@ def worst_error(specs, refs):
     return worst
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "simt"])
 @pytest.mark.parametrize("graph", [False, True])
 def test_config4_grouped_256_problems(prec, graph):
     shapes = workloads.grouped_shapes()
@@ -66,7 +66,7 @@ def test_config4_grouped_256_problems(prec, graph):
     plan.close()
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9", "fp16x3", "simt"])
 def test_grouped_edge_cases(prec):
     """Tiny, ragged, K = 0, alpha = 0 and padded leading dimensions."""
     shapes = [("N", "N", 1, 1, 1), ("T", "T", 3, 5, 7), ("N", "T", 129, 257, 33),
@@ -85,7 +85,7 @@ def test_grouped_edge_cases(prec):
         assert torch.equal(s["C"][:, s["N"]:], k)  # padding untouched
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "simt"])
 def test_grouped_split_k_slices_deep_problems(prec):
     """Weight-gradient-shaped problems (small output, k in the tens of
     thousands) beside shallow ones: the plan cuts the deep ones into k
@@ -121,7 +121,7 @@ def test_grouped_split_k_slices_deep_problems(prec):
     plan.close()
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9"])
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9", "fp16x3"])
 def test_grouped_wide_and_narrow_problems(prec):
     """Few rows and many columns (computed transposed by the split form) and
     narrow right-edge tiles (MMAs as wide as the columns, in steps of 16)."""

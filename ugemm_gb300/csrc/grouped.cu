@@ -64,7 +64,7 @@ struct ugemm_grouped_plan_s {
   int device = 0;
   double flops = 0;
   // device memory
-  void* table = nullptr;    // maps | problems | jobs
+  void* table = nullptr;    // maps | problems | jobs | reduce jobs | tile records | max words
   void* scratch = nullptr;  // operand slots
   int* dev_err = nullptr;
   const CUtensorMap* maps = nullptr;
@@ -74,6 +74,7 @@ struct ugemm_grouped_plan_s {
   int nsub = 0;                   // kernel problems (split-K slices count one each)
   const void* reduce = nullptr;   // split-K reduce jobs
   const int4* tiles = nullptr;    // split form: per-CTA ranges, then one record per tile
+  unsigned* fmax = nullptr;       // FP16x3: the operands' largest magnitudes, two per problem
   int grid = 0;                   // split form: persistent CTAs the tile table is dealt to
   int nreduce = 0;
   long long reduce_max = 0;       // largest M x N among them
@@ -108,7 +109,7 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
     return s == UGEMM_OK ? reduce_launch(p, st) : s;
   }
   s = split_batched_launch(p->split.pieces, static_cast<const SplitJob*>(p->jobs), p->njobs,
-                           p->prep_tiles, st);
+                           p->prep_tiles, st, p->fmax, p->fmax ? 2 * p->count : 0);
   if (s != UGEMM_OK) return s;
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
@@ -164,7 +165,7 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   if (count <= 0 || !problems) return plan_fail(UGEMM_ERR_ARG, "empty problem list");
   int form = precision;
   if (form == UGEMM_PREC_AUTO) form = UGEMM_PREC_BF16X6;
-  if (form < UGEMM_PREC_SIMT || form > UGEMM_PREC_BF16X3)
+  if (form < UGEMM_PREC_SIMT || form > UGEMM_PREC_FP16X3)
     return plan_fail(UGEMM_ERR_ARG, "unknown precision");
   // validate and normalise
   std::vector<Gemm> g(count);
@@ -355,7 +356,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
       SplitJob bj{x.B, b_sr, b_sk, reinterpret_cast<__nv_bfloat16*>(base + b_off[j]), x.N, x.K, kp,
                   prep};
       if (gather) { bj.gather = gather; bj.im = *x.b_im2col; }
-      sjobs.push_back(bj);
+      sjobs.push_back(bj);  // FP16x3: fmax words are set once the table exists
       prep += cdiv(x.N, 32) * tk;
     }
   }
@@ -456,7 +457,27 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   }
   const size_t rec_bytes = recs.size() * sizeof(int4);
   const size_t off_t = off_r + align_up(std::max<size_t>(red_bytes, 1), 256);
-  const size_t total = off_t + align_up(std::max<size_t>(rec_bytes, 1), 256);
+  // FP16x3: the operands' largest magnitudes, cleared on every run
+  const bool f16 = !simt && p->split.f16;
+  const size_t off_w = off_t + align_up(std::max<size_t>(rec_bytes, 1), 256);
+  const size_t total = off_w + (f16 ? align_up(2 * size_t(count) * sizeof(unsigned), 256) : 0);
+  e = cudaMalloc(&p->table, total);
+  if (e != cudaSuccess) {
+    free_plan(p);
+    return plan_fail(UGEMM_ERR_ALLOC, "grouped plan table allocation failed");
+  }
+  uint8_t* tb = static_cast<uint8_t*>(p->table);
+  if (f16) {  // operand j's word: jobs 2j (A) and 2j + 1 (B) fill it, its problems read it
+    unsigned* words = reinterpret_cast<unsigned*>(tb + off_w);
+    p->fmax = words;
+    for (size_t q = 0; q < sjobs.size(); ++q) sjobs[q].fmax = words + q;
+    for (size_t i = 0; i < tprobs.size(); ++i) {
+      const int j = subs[i].j;
+      const bool sw = geo[j].swap;  // kernel operand a is op(B)^T's pieces when swapped
+      tprobs[i].fmax_a = words + 2 * j + (sw ? 1 : 0);
+      tprobs[i].fmax_b = words + 2 * j + (sw ? 0 : 1);
+    }
+  }
   std::vector<uint8_t> host(total, 0);
   std::memcpy(host.data(), maps.data(), maps_bytes);
   std::memcpy(host.data() + off_p, simt ? static_cast<const void*>(sprobs.data()) : tprobs.data(),
@@ -465,13 +486,11 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
               job_bytes);
   if (red_bytes) std::memcpy(host.data() + off_r, rjobs.data(), red_bytes);
   if (rec_bytes) std::memcpy(host.data() + off_t, recs.data(), rec_bytes);
-  e = cudaMalloc(&p->table, total);
-  if (e == cudaSuccess) e = cudaMemcpy(p->table, host.data(), total, cudaMemcpyHostToDevice);
+  e = cudaMemcpy(p->table, host.data(), total, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     free_plan(p);
     return plan_fail(UGEMM_ERR_ALLOC, "grouped plan table upload failed");
   }
-  uint8_t* tb = static_cast<uint8_t*>(p->table);
   p->maps = reinterpret_cast<const CUtensorMap*>(tb);
   p->probs = tb + off_p;
   p->jobs = tb + off_j;

@@ -772,7 +772,7 @@ __device__ __forceinline__ void tile_origin(const SplitJob& j, int b, int& r0, i
   k0 = (local % tiles_k) * 64;
 }
 
-template <int NP>
+template <int NP, bool F16>
 __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
                                                                    int njobs, int total_tiles) {
   __shared__ float tile[32][65];
@@ -798,12 +798,61 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
       load_raw(nxt, nr0, nk0, raw);
     }
     __syncthreads();
-    split_store<NP, false>(cur, r0, k0, tile);
+    split_store<NP, F16>(cur, r0, k0, tile);
     __syncthreads();
     cur = nxt;
     r0 = nr0;
     k0 = nk0;
   }
+}
+
+// FP16x3 form of the batched pre-pass, first step: the largest magnitude of
+// every job's operand (the same 32 x 64 tiles and loads as the split,
+// implicit im2col gathers included) folded into its `fmax` word.  A block
+// keeps a running maximum while its tiles belong to one job and folds it
+// with one atomicMax when the job changes, so a large operand costs one
+// atomic per block, not one per tile.
+__global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob* __restrict__ jobs,
+                                                                  int njobs, int total_tiles) {
+  __shared__ int starts[kJobCache];
+  __shared__ float warp_max[8];
+  const int cached = min(njobs, kJobCache);
+  for (int i = threadIdx.x; i < cached; i += blockDim.x) starts[i] = jobs[i].tile_start;
+  __syncthreads();
+  float m = 0.f;
+  int cur = -1;
+  unsigned* word = nullptr;
+  auto fold = [&]() {  // every thread of the block, between tiles
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float v = warp_max[0];
+      for (int w = 1; w < 8; ++w) v = fmaxf(v, warp_max[w]);
+      if (v > 0.f) atomicMax(word, __float_as_uint(v));
+    }
+    __syncthreads();
+    m = 0.f;
+  };
+  for (int b = blockIdx.x; b < total_tiles; b += gridDim.x) {
+    const int ji = find_job(starts, jobs, njobs, b);
+    if (ji != cur) {
+      if (cur >= 0) fold();
+      cur = ji;
+      word = jobs[ji].fmax;
+    }
+    const SplitJob j = jobs[ji];
+    int r0, k0;
+    tile_origin(j, b, r0, k0);
+    RawTile raw;
+    load_raw(j, r0, k0, raw);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) m = fmaxf(m, fabsf(raw.v[i][e]));
+  }
+  if (cur >= 0) fold();
 }
 
 template <int NP>
@@ -1041,12 +1090,24 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
 }
 
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, unsigned* fmax_words, int nwords) {
   if (total_tiles <= 0) return UGEMM_OK;
   const int grid = std::min(total_tiles, sm_count() * 8);
+  if (fmax_words) {  // FP16x3: every job's largest magnitude first
+    if (pieces != 2) return UGEMM_ERR_ARG;
+    if (cudaMemsetAsync(fmax_words, 0, sizeof(unsigned) * nwords, st) != cudaSuccess)
+      return UGEMM_ERR_CUDA;
+    prof_begin(st);
+    operand_max_batched_kernel<<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+    prof_end(st, kProfSplitPrep);
+    prof_begin(st);
+    split_pieces_batched_kernel<2, true><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+    prof_end(st, kProfSplitPrep);
+    return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+  }
   prof_begin(st);
-  if (pieces == 3) split_pieces_batched_kernel<3><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
-  else split_pieces_batched_kernel<2><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  if (pieces == 3) split_pieces_batched_kernel<3, false><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  else split_pieces_batched_kernel<2, false><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
   prof_end(st, kProfSplitPrep);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }

@@ -121,9 +121,10 @@ struct SplitJob {
   // 2 = rows are taps and k pixels; 0 = plain strided matrix
   int gather = 0;
   Im2col im;
-  // FP16x3 form: the operand's largest magnitude (operand_max_launch), from
-  // which the pieces' power-of-two scale follows; null: bf16 pieces.
-  const unsigned* fmax = nullptr;
+  // FP16x3 form: the word that receives the operand's largest magnitude
+  // (operand_max_batched_kernel), from which the pieces' power-of-two scale
+  // follows; null: bf16 pieces.
+  unsigned* fmax = nullptr;
 };
 
 int split_kp(int K);
@@ -169,8 +170,11 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
 // per tile (raster order within a problem), dealt longest first to the
 // least-loaded CTA.
 std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid);
+// The batched pre-pass of a grouped plan.  fmax_words (FP16x3 plans): the
+// jobs' `fmax` words, nwords of them contiguous, cleared and filled before
+// the split.
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
-                                  cudaStream_t st);
+                                  cudaStream_t st, unsigned* fmax_words = nullptr, int nwords = 0);
 // Split one operand into its pieces at dst (split_operand_bytes of room).
 // f16: FP16x3 pieces -- the largest magnitude is first found into the
 // operand's trailer word (cleared here), then the pieces are scaled by it.
