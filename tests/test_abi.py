@@ -52,6 +52,21 @@ def test_only_c_abi_symbols_are_exported(lib):
     assert set(header_functions()) <= ours
 
 
+def header_enum(prefix):
+    text = open(os.path.join(ROOT, "include", "sgemm_cuda.h")).read()
+    return {m.group(1): int(m.group(2))
+            for m in re.finditer(r"\b(" + prefix + r"[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+
+
+def test_python_constants_match_the_header():
+    """The host mirror's status codes and arithmetic forms are the header's."""
+    forms = header_enum("UGEMM_PREC_")
+    assert forms == {f"UGEMM_PREC_{k.upper()}": v for k, v in ug.PRECISIONS.items()}
+    status = header_enum("UGEMM_ERR_")
+    for name, value in status.items():
+        assert getattr(ug, name[len("UGEMM_"):]) == value, name
+
+
 def test_status_strings(lib):
     assert lib.ugemm_status_string(0) == b"ok"
     assert b"argument" in lib.ugemm_status_string(ug.ERR_ARG)
