@@ -31,7 +31,9 @@
 //   2. GEMM kernel, 10 warps:
 //        warp 0   TMA producer: one 3-D TMA per operand per stage brings all
 //                 pieces of a 32-deep k slice (64-byte swizzle) into a 3-4
-//                 stage ring (mbarrier full/empty pairs);
+//                 stage ring (mbarrier full/empty pairs) -- for one GEMM of
+//                 two-piece operands a 64-deep slice (128-byte swizzle) into
+//                 a 2-3 stage ring, which halves the per-stage overhead;
 //        warp 1   allocates TMEM (2 x BN columns: main + corrections) and,
 //                 from one thread, issues the tcgen05.mma stream;
 //        warps 2-9  epilogue: chunk drains, then alpha/beta and the store of
@@ -118,7 +120,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                     int total_tiles, int nprod,
                     int chunk_kb, int f16, int* err) {
-  using S = TcShape<NP, BN>;
+  constexpr bool WIDE = split_stage_k(NP, GROUPED) > kTcKB;
+  using S = TcShape<NP, BN, WIDE>;
+  constexpr int KB = S::KB;
+  // K-major operand tiles: 8-row groups of 128-byte rows (128-byte swizzle)
+  // or of 64-byte rows (64-byte swizzle); one k16 MMA step is 32 bytes
+  constexpr uint32_t SBO = WIDE ? 1024 : 512, SWZ = WIDE ? 2 : 4;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S::STAGES * S::STAGE_BYTES);
@@ -180,8 +187,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
           uint8_t* sa = smem + s * S::STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_3d(sa, ma, &full[s], (kb0 + kb) * kTcKB, tc.m0, 0);
-          tma_load_3d(sa + S::A_BYTES, mb, &full[s], (kb0 + kb) * kTcKB, tc.n0, 0);
+          tma_load_3d(sa, ma, &full[s], (kb0 + kb) * KB, tc.m0, 0);
+          tma_load_3d(sa + S::A_BYTES, mb, &full[s], (kb0 + kb) * KB, tc.n0, 0);
         }
       }
       if (!ok) {  // let copies still in flight land before the CTA exits
@@ -230,9 +237,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t code = kCorrections[p];
             const uint32_t ia = code >> 2, ib = code & 3;
 #pragma unroll
-            for (int kk = 0; kk < kTcKB / 16; ++kk)
-              umma_bf16(t_corr, umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, 512, 4),
-                        umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, 512, 4), idesc,
+            for (int kk = 0; kk < KB / 16; ++kk)
+              umma_bf16(t_corr, umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, SBO, SWZ),
+                        umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, SBO, SWZ), idesc,
                         (kb | p | kk) != 0);
           }
           // main product; a new chunk restarts the accumulator once drained
@@ -246,9 +253,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             tc_fence_after();
           }
 #pragma unroll
-          for (int kk = 0; kk < kTcKB / 16; ++kk)
-            umma_bf16(t_main, umma_smem_desc(sa + kk * 32, 512, 4),
-                      umma_smem_desc(sb + kk * 32, 512, 4), idesc, !(chunk_start && kk == 0));
+          for (int kk = 0; kk < KB / 16; ++kk)
+            umma_bf16(t_main, umma_smem_desc(sa + kk * 32, SBO, SWZ),
+                      umma_smem_desc(sb + kk * 32, SBO, SWZ), idesc, !(chunk_start && kk == 0));
           umma_commit(&empty[s]);
           if ((kb + 1) % chunk_kb == 0 && kb + 1 < P.nkb) umma_commit(&main_full[buf]);
         }
@@ -887,7 +894,7 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
                            const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
                            int total_tiles, int nprod, int chunk_kb, int max_ctas, bool f16,
                            int* dev_err, cudaStream_t st) {
-  using S = TcShape<NP, BN>;
+  using S = TcShape<NP, BN, (split_stage_k(NP, GROUPED) > kTcKB)>;
   auto kern = split_tc_kernel<NP, BN, GROUPED, EPI>;
   static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
   if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
@@ -989,13 +996,15 @@ bool split_encode_view(int pieces, int box_rows, const void* base, int rows, int
 }
 
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
-                       int K, CUtensorMap* ta, CUtensorMap* tb) {
+                       int K, CUtensorMap* ta, CUtensorMap* tb, bool wide) {
   const int Kp = kp_of(K);
   const uint64_t row = uint64_t(Kp) * 2;
+  const uint32_t kb = wide ? 2 * kTcKB : kTcKB;
+  const CUtensorMapSwizzle sw = wide ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
   return encode_tmap_3d(ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ap, Kp, M, pieces, row, row * M,
-                        kTcKB, kTcBM, pieces, CU_TENSOR_MAP_SWIZZLE_64B) &&
+                        kb, kTcBM, pieces, sw) &&
          encode_tmap_3d(tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bp, Kp, N, pieces, row, row * N,
-                        kTcKB, block_n, pieces, CU_TENSOR_MAP_SWIZZLE_64B);
+                        kb, block_n, pieces, sw);
 }
 
 TcProblem split_problem(const Gemm& g, int block_n, int tile_start) {
@@ -1044,16 +1053,22 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
     launch_split<2>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
     launch_split<2>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
   }
+  // the one-GEMM kernel's stage depth (the wave tail below keeps 32)
+  const int kstage = split_stage_k(p.pieces, false);
+  const bool wide = kstage > kTcKB;
   CUtensorMap ta, tb;
-  if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb))
+  if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb, wide))
     return UGEMM_ERR_CUDA;
   TcProblem P = split_problem(g, p.block_n, 0);
+  P.nkb = cdiv(Kp, kstage);
   if (p.f16) {
     P.fmax_a = split_fmax_word(ap, 2, g.M, g.K);
     P.fmax_b = split_fmax_word(bp, 2, g.N, g.K);
   }
   const int total = P.tiles_m * P.tiles_n;
-  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  // chunk length in the kernel's stages (the same k depth as in 32-deep ones)
+  const int chunk = std::max(1, (p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb()) /
+                                    (kstage / kTcKB));
   // a partial last wave of tiles runs as two k slices (multi.cu)
   const TailPlan tail = tail_plan(g, p);
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
@@ -1152,15 +1167,19 @@ ugemm_status split_operand_launch(int pieces, const float* src, long long sr, lo
 ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
                                   const void* b_pieces, void* tail_scratch, int* dev_err,
                                   cudaStream_t st) {
+  const int kstage = split_stage_k(p.pieces, false);
+  const bool wide = kstage > kTcKB;
   CUtensorMap ta, tb;
-  if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb))
+  if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb, wide))
     return UGEMM_ERR_CUDA;
   TcProblem P = split_problem(g, p.block_n, 0);
+  P.nkb = cdiv(kp_of(g.K), kstage);
   if (p.f16) {
     P.fmax_a = split_fmax_word(a_pieces, 2, g.M, g.K);
     P.fmax_b = split_fmax_word(b_pieces, 2, g.N, g.K);
   }
-  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  const int chunk = std::max(1, (p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb()) /
+                                    (kstage / kTcKB));
   const TailPlan tail = tail_scratch ? tail_plan(g, p) : TailPlan{};
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
                                      tail.use ? tail.main_tiles : P.tiles_m * P.tiles_n, chunk, 0,

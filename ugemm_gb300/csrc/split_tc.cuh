@@ -59,10 +59,17 @@ __host__ __device__ __forceinline__ void tc_raster(int local, int tiles_m, int t
   n0 = ((local % per_group) / group_rows) * block_n;
 }
 
-template <int NP, int BN>
+// WIDE: 64-deep stages of 128-byte rows (128-byte swizzle) instead of
+// 32-deep ones of 64-byte rows.  Each stage carries a fixed cost on top of
+// its MMAs (measured: ~0.26 us per stage whatever its MMA count), so the
+// three-product form, with few MMAs per k, takes two k-blocks per stage;
+// its stage (96 KB at BN = 256) leaves room for two.  Only one-GEMM launches
+// of two-piece operands use it (split_stage_k).
+template <int NP, int BN, bool WIDE = false>
 struct TcShape {
-  static constexpr int A_PLANE = kTcBM * kTcKB * 2;  // bytes of one A piece tile
-  static constexpr int B_PLANE = BN * kTcKB * 2;
+  static constexpr int KB = WIDE ? 2 * kTcKB : kTcKB;  // k depth of a stage
+  static constexpr int A_PLANE = kTcBM * KB * 2;  // bytes of one A piece tile
+  static constexpr int B_PLANE = BN * KB * 2;
   static constexpr int A_BYTES = NP * A_PLANE;
   static constexpr int B_BYTES = NP * B_PLANE;
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
@@ -97,7 +104,7 @@ struct TcProblem {
   float* C;
   int M, N, ldc;
   float alpha, beta;
-  int nkb;              // k-blocks of kTcKB
+  int nkb;              // stages of the kernel's k depth (split_stage_k)
   int tiles_m, tiles_n;
   int tile_start;       // first global tile index of this problem
   int kb0 = 0;
@@ -136,8 +143,15 @@ size_t split_operand_bytes(int pieces, int rows, int K);
 unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K);
 void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
                            long long* b_sk);
+// wide: boxes of a 64-deep stage with the 128-byte swizzle (the two-piece
+// one-GEMM kernel); otherwise 32-deep with the 64-byte swizzle.
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
-                       int K, CUtensorMap* ta, CUtensorMap* tb);
+                       int K, CUtensorMap* ta, CUtensorMap* tb, bool wide = false);
+// k depth of one pipeline stage of a launch: 64 for one GEMM of two-piece
+// operands, 32 otherwise (grouped launches, three-piece operands).
+constexpr int split_stage_k(int pieces, bool grouped) {
+  return (pieces == 2 && !grouped) ? 2 * kTcKB : kTcKB;
+}
 TcProblem split_problem(const Gemm& g, int block_n, int tile_start);
 // Map of rows [0, rows) of a piece array whose planes are plane_rows long
 // (a view starting inside the array: base points at its first row).
