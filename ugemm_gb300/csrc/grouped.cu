@@ -116,7 +116,8 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
   TcProblem single{};
   s = split_gemm_launch(p->split, dummy, dummy, single, p->maps,
                         static_cast<const TcProblem*>(p->probs), p->tiles, p->gemm_tiles,
-                        std::max(1, p->cfg.chunk_k / kTcKB), p->grid, p->dev_err, st);
+                        split_chunk_stages(p->split.pieces, std::max(1, p->cfg.chunk_k / kTcKB)),
+                        p->grid, p->dev_err, st);
   return s == UGEMM_OK ? reduce_launch(p, st) : s;
 }
 
@@ -263,7 +264,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
       o.swap = padded_area(x.N, x.M, bn) < padded_area(x.M, x.N, bn);
       const int rows = o.swap ? x.N : x.M, cols = o.swap ? x.M : x.N;
       o.tiles = cdiv(rows, kTcBM) * cdiv(cols, bn);
-      o.nkb = split_kp(x.K) / kTcKB;
+      o.nkb = split_nkb(pieces, x.K);
     }
     o.per = o.nkb;
     work += double(o.tiles) * o.nkb;
@@ -271,17 +272,19 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   // Split-K.  The persistent CTAs share the group's tile k-blocks; a problem
   // whose tiles are each longer than half an SM's fair share (a weight
   // gradient: small output, k = batch x pixels) would leave most SMs idle,
-  // so it is cut into slices of about that length, at least kMinSlice
+  // so it is cut into slices of about that length, at least min_slice
   // k-blocks, and at most 1 GiB of partial tiles.
-  constexpr int kMinSlice = 16;
+  // (stages: 16 k-blocks of 32 in the SIMT form and the three-piece split
+  // form, 8 of 64 for two-piece operands)
+  const int min_slice = 16 * kTcKB / (simt ? kTcKB : split_stage_k(pieces));
   const double fair = work / (2.0 * sms);
   std::vector<size_t> part_off(count, 0);
   size_t part_bytes = 0;
   for (int j = 0; j < count; ++j) {
     const Gemm& x = g[order[j]];
     Geo& o = geo[j];
-    if (x.K == 0 || o.nkb < 2 * kMinSlice || o.nkb <= fair) continue;
-    const int len = std::max(kMinSlice, static_cast<int>(fair) + 1);
+    if (x.K == 0 || o.nkb < 2 * min_slice || o.nkb <= fair) continue;
+    const int len = std::max(min_slice, static_cast<int>(fair) + 1);
     const size_t tile_bytes = size_t(x.M) * x.N * 4;
     int sl = std::min(cdiv(o.nkb, len), 256);
     sl = static_cast<int>(std::min<size_t>(sl, (size_t(1) << 30) / tile_bytes));

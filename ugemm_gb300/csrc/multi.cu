@@ -28,6 +28,9 @@ namespace {
 constexpr int kMultiSubs = 24;  // kernel problems (slices) per launch
 constexpr int kMinSlice = 16;   // shortest slice, in 32-deep k-blocks
 
+// The shortest slice in stages of the kernel's k depth.
+int min_slice(int pieces) { return kMinSlice * kTcKB / split_stage_k(pieces); }
+
 // Everything the launch reads from device memory, filled by one small kernel
 // from its by-value parameter (at most 4 KB of parameters).
 struct MultiTable {
@@ -109,7 +112,7 @@ Layout layout_for(const Gemm* gs, int n, const SplitPlan& p, int sms) {
     o.swap = padded(g.N, g.M, L.block_n) < padded(g.M, g.N, L.block_n);
     const int rows = o.swap ? g.N : g.M, cols = o.swap ? g.M : g.N;
     o.tiles = cdiv(rows, kTcBM) * cdiv(cols, L.block_n);
-    o.nkb = split_kp(g.K) / kTcKB;
+    o.nkb = split_nkb(p.pieces, g.K);
     o.per = o.nkb;
     work += double(o.tiles) * o.nkb;
   }
@@ -119,8 +122,8 @@ Layout layout_for(const Gemm* gs, int n, const SplitPlan& p, int sms) {
   for (int i = 0; i < n; ++i) {
     const Gemm& g = gs[i];
     Geo& o = L.geo[i];
-    if (o.nkb < 2 * kMinSlice || o.nkb <= fair) continue;
-    const int len = std::max(kMinSlice, static_cast<int>(fair) + 1);
+    if (o.nkb < 2 * min_slice(p.pieces) || o.nkb <= fair) continue;
+    const int len = std::max(min_slice(p.pieces), static_cast<int>(fair) + 1);
     const size_t tile_bytes = size_t(g.M) * g.N * 4;
     int sl = std::min(cdiv(o.nkb, len), kMultiSubs - (subs - 1));
     sl = static_cast<int>(std::min<size_t>(sl, (size_t(512) << 20) / tile_bytes));
@@ -157,7 +160,7 @@ TailPlan tail_plan(const Gemm& g, const SplitPlan& p) {
   const int sms = sm_count();
   const int tiles_m = cdiv(g.M, kTcBM), tiles_n = cdiv(g.N, p.block_n);
   const int tiles = tiles_m * tiles_n, rem = tiles % sms;
-  if (tiles <= sms || rem == 0 || split_kp(g.K) / kTcKB < 2 * kMinSlice) return t;
+  if (tiles <= sms || rem == 0 || split_nkb(p.pieces, g.K) < 2 * min_slice(p.pieces)) return t;
   // the raster order ends with the last group of tile rows, column by column
   const int first_m = ((tiles_m - 1) / kTcRaster) * kTcRaster, rows = tiles_m - first_m;
   const int cols = cdiv(rem, rows);             // whole tile columns of that group
@@ -193,7 +196,7 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
   if (!split_encode_view(p.pieces, kTcBM, ap, Mt, g.M, g.K, &t.maps[0]) ||
       !split_encode_view(p.pieces, p.block_n, bp, Nt, g.N, g.K, &t.maps[1]))
     return UGEMM_ERR_CUDA;
-  const int nkb = Kp / kTcKB, per = cdiv(nkb, 2);
+  const int nkb = split_nkb(p.pieces, g.K), per = cdiv(nkb, 2);
   int tiles = 0;
   for (int s = 0; s < 2; ++s) {
     TcProblem& tp = t.probs[s];
@@ -226,7 +229,8 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
-  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  const int chunk =
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
   ugemm_status s = split_gemm_launch(
       q, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
       reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), recs, tiles, chunk,
@@ -239,7 +243,7 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
 bool multi_wanted(const Gemm& g, const SplitPlan& p) {
   if (g.M == 0 || g.N == 0 || g.K == 0 || g.alpha == 0.f) return false;
   const int tiles = cdiv(g.M, kTcBM) * cdiv(g.N, p.block_n);
-  return tiles < sm_count() && split_kp(g.K) / kTcKB >= 2 * kMinSlice;
+  return tiles < sm_count() && split_nkb(p.pieces, g.K) >= 2 * min_slice(p.pieces);
 }
 
 size_t multi_scratch_bytes(const Gemm* gs, int n, const SplitPlan& p) {
@@ -323,7 +327,8 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
-  const int chunk = p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb();
+  const int chunk =
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
   ugemm_status s = split_gemm_launch(
       p, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
       reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), recs, tiles, chunk,

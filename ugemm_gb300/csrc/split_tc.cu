@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                     int total_tiles, int nprod,
                     int chunk_kb, int f16, int* err) {
-  constexpr bool WIDE = split_stage_k(NP, GROUPED) > kTcKB;
+  constexpr bool WIDE = split_stage_k(NP) > kTcKB;
   using S = TcShape<NP, BN, WIDE>;
   constexpr int KB = S::KB;
   // K-major operand tiles: 8-row groups of 128-byte rows (128-byte swizzle)
@@ -894,7 +894,7 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
                            const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
                            int total_tiles, int nprod, int chunk_kb, int max_ctas, bool f16,
                            int* dev_err, cudaStream_t st) {
-  using S = TcShape<NP, BN, (split_stage_k(NP, GROUPED) > kTcKB)>;
+  using S = TcShape<NP, BN, (split_stage_k(NP) > kTcKB)>;
   auto kern = split_tc_kernel<NP, BN, GROUPED, EPI>;
   static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
   if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
@@ -987,27 +987,34 @@ size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p) {
          tail_scratch_bytes(g, p);
 }
 
+// Boxes of one stage: split_stage_k(pieces) deep, 128-byte swizzle for
+// 64-deep stages, 64-byte swizzle for 32-deep ones.
+CUtensorMapSwizzle split_swizzle(int pieces) {
+  return split_stage_k(pieces) > kTcKB ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+}
+
 bool split_encode_view(int pieces, int box_rows, const void* base, int rows, int plane_rows, int K,
                        CUtensorMap* map) {
   const int Kp = kp_of(K);
   const uint64_t row = uint64_t(Kp) * 2;
   return encode_tmap_3d(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, Kp, rows, pieces, row,
-                        row * plane_rows, kTcKB, box_rows, pieces, CU_TENSOR_MAP_SWIZZLE_64B);
+                        row * plane_rows, split_stage_k(pieces), box_rows, pieces,
+                        split_swizzle(pieces));
 }
 
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
-                       int K, CUtensorMap* ta, CUtensorMap* tb, bool wide) {
+                       int K, CUtensorMap* ta, CUtensorMap* tb) {
   const int Kp = kp_of(K);
   const uint64_t row = uint64_t(Kp) * 2;
-  const uint32_t kb = wide ? 2 * kTcKB : kTcKB;
-  const CUtensorMapSwizzle sw = wide ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  const uint32_t kb = split_stage_k(pieces);
+  const CUtensorMapSwizzle sw = split_swizzle(pieces);
   return encode_tmap_3d(ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ap, Kp, M, pieces, row, row * M,
                         kb, kTcBM, pieces, sw) &&
          encode_tmap_3d(tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bp, Kp, N, pieces, row, row * N,
                         kb, block_n, pieces, sw);
 }
 
-TcProblem split_problem(const Gemm& g, int block_n, int tile_start) {
+TcProblem split_problem(const Gemm& g, int pieces, int block_n, int tile_start) {
   TcProblem P;
   P.C = g.C;
   P.M = g.M;
@@ -1015,7 +1022,7 @@ TcProblem split_problem(const Gemm& g, int block_n, int tile_start) {
   P.ldc = g.ldc;
   P.alpha = g.alpha;
   P.beta = g.beta;
-  P.nkb = kp_of(g.K) / kTcKB;
+  P.nkb = split_nkb(pieces, g.K);
   P.tiles_m = cdiv(g.M, kTcBM);
   P.tiles_n = cdiv(g.N, block_n);
   P.tile_start = tile_start;
@@ -1053,22 +1060,17 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
     launch_split<2>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
     launch_split<2>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
   }
-  // the one-GEMM kernel's stage depth (the wave tail below keeps 32)
-  const int kstage = split_stage_k(p.pieces, false);
-  const bool wide = kstage > kTcKB;
   CUtensorMap ta, tb;
-  if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb, wide))
+  if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb))
     return UGEMM_ERR_CUDA;
-  TcProblem P = split_problem(g, p.block_n, 0);
-  P.nkb = cdiv(Kp, kstage);
+  TcProblem P = split_problem(g, p.pieces, p.block_n, 0);
   if (p.f16) {
     P.fmax_a = split_fmax_word(ap, 2, g.M, g.K);
     P.fmax_b = split_fmax_word(bp, 2, g.N, g.K);
   }
   const int total = P.tiles_m * P.tiles_n;
-  // chunk length in the kernel's stages (the same k depth as in 32-deep ones)
-  const int chunk = std::max(1, (p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb()) /
-                                    (kstage / kTcKB));
+  const int chunk =
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
   // a partial last wave of tiles runs as two k slices (multi.cu)
   const TailPlan tail = tail_plan(g, p);
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
@@ -1167,19 +1169,16 @@ ugemm_status split_operand_launch(int pieces, const float* src, long long sr, lo
 ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void* a_pieces,
                                   const void* b_pieces, void* tail_scratch, int* dev_err,
                                   cudaStream_t st) {
-  const int kstage = split_stage_k(p.pieces, false);
-  const bool wide = kstage > kTcKB;
   CUtensorMap ta, tb;
-  if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb, wide))
+  if (!split_encode_maps(p.pieces, p.block_n, a_pieces, g.M, b_pieces, g.N, g.K, &ta, &tb))
     return UGEMM_ERR_CUDA;
-  TcProblem P = split_problem(g, p.block_n, 0);
-  P.nkb = cdiv(kp_of(g.K), kstage);
+  TcProblem P = split_problem(g, p.pieces, p.block_n, 0);
   if (p.f16) {
     P.fmax_a = split_fmax_word(a_pieces, 2, g.M, g.K);
     P.fmax_b = split_fmax_word(b_pieces, 2, g.N, g.K);
   }
-  const int chunk = std::max(1, (p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb()) /
-                                    (kstage / kTcKB));
+  const int chunk =
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
   const TailPlan tail = tail_scratch ? tail_plan(g, p) : TailPlan{};
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
                                      tail.use ? tail.main_tiles : P.tiles_m * P.tiles_n, chunk, 0,

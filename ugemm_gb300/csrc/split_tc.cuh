@@ -62,9 +62,8 @@ __host__ __device__ __forceinline__ void tc_raster(int local, int tiles_m, int t
 // WIDE: 64-deep stages of 128-byte rows (128-byte swizzle) instead of
 // 32-deep ones of 64-byte rows.  Each stage carries a fixed cost on top of
 // its MMAs (measured: ~0.26 us per stage whatever its MMA count), so the
-// three-product form, with few MMAs per k, takes two k-blocks per stage;
-// its stage (96 KB at BN = 256) leaves room for two.  Only one-GEMM launches
-// of two-piece operands use it (split_stage_k).
+// two-piece forms, with few MMAs per k, take two k-blocks per stage; their
+// stage (96 KB at BN = 256) leaves room for two (split_stage_k).
 template <int NP, int BN, bool WIDE = false>
 struct TcShape {
   static constexpr int KB = WIDE ? 2 * kTcKB : kTcKB;  // k depth of a stage
@@ -143,16 +142,22 @@ size_t split_operand_bytes(int pieces, int rows, int K);
 unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K);
 void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
                            long long* b_sk);
-// wide: boxes of a 64-deep stage with the 128-byte swizzle (the two-piece
-// one-GEMM kernel); otherwise 32-deep with the 64-byte swizzle.
-bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
-                       int K, CUtensorMap* ta, CUtensorMap* tb, bool wide = false);
-// k depth of one pipeline stage of a launch: 64 for one GEMM of two-piece
-// operands, 32 otherwise (grouped launches, three-piece operands).
-constexpr int split_stage_k(int pieces, bool grouped) {
-  return (pieces == 2 && !grouped) ? 2 * kTcKB : kTcKB;
+// k depth of one pipeline stage: 64 for two-piece operands (128-byte
+// swizzle), 32 for three-piece ones (64-byte swizzle).  The tensor maps'
+// boxes and every launch's TcProblem::nkb follow it.
+constexpr int split_stage_k(int pieces) { return pieces == 2 ? 2 * kTcKB : kTcKB; }
+// Stages of the kernel's depth over K, and a chunk of `chunk_kb` 32-deep
+// k-blocks in stages.
+inline int split_nkb(int pieces, int K) {
+  return (split_kp(K) + split_stage_k(pieces) - 1) / split_stage_k(pieces);
 }
-TcProblem split_problem(const Gemm& g, int block_n, int tile_start);
+inline int split_chunk_stages(int pieces, int chunk_kb) {
+  const int c = chunk_kb / (split_stage_k(pieces) / kTcKB);
+  return c > 0 ? c : 1;
+}
+bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
+                       int K, CUtensorMap* ta, CUtensorMap* tb);
+TcProblem split_problem(const Gemm& g, int pieces, int block_n, int tile_start);
 // Map of rows [0, rows) of a piece array whose planes are plane_rows long
 // (a view starting inside the array: base points at its first row).
 bool split_encode_view(int pieces, int box_rows, const void* base, int rows, int plane_rows, int K,
