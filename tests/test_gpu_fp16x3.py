@@ -1,7 +1,8 @@
 """The FP16x3 split form: each operand is scaled by a power of two chosen from
 its largest magnitude and written as two fp16 pieces.  These cases check the
 scale logic where it matters -- operands far above fp16's range, far below
-it, one outlier element, an all-zero operand -- against an FP64 GEMM, and
+it, one outlier element, an infinity, an all-zero operand -- against an
+FP64 GEMM, and
 that the form matches BF16x6 and the FP32 SIMT form on ordinary inputs."""
 import math
 
@@ -76,6 +77,23 @@ def test_outlier_element_sets_the_scale():
     ref = ref64("N", "N", A, B, C0, 1.0, 0.0)
     got = gemm("N", "N", A, B, C0, 1.0, 0.0, "fp16x3")
     assert nerr(got, ref) < TOL
+
+
+def test_infinity_does_not_set_the_scale():
+    """An infinite element propagates into its own row of C only: the scale
+    follows the finite elements, so the rest of a large-valued operand
+    (1e6: unscaled it would overflow fp16) stays accurate."""
+    g = torch.Generator(device="cuda").manual_seed(8)
+    M, N, K = 130, 140, 300
+    A = uniform((M, K), g, 1e6)
+    A[0, 5] = float("inf")
+    B = uniform((K, N), g)
+    C0 = torch.zeros((M, N), device="cuda")
+    got = gemm("N", "N", A, B, C0, 1.0, 0.0, "fp16x3")
+    assert not torch.isfinite(got[0]).any()
+    ref = ref64("N", "N", A[1:], B, C0[1:], 1.0, 0.0)
+    assert torch.isfinite(got[1:]).all()
+    assert nerr(got[1:], ref) < TOL
 
 
 def test_zero_operand_gives_beta_c():

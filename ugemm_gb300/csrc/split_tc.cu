@@ -45,6 +45,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cfloat>
+
 #include <algorithm>
 #include <cstdlib>
 #include <functional>
@@ -503,6 +505,14 @@ __device__ __forceinline__ void pieces_pair(float x0, float x1, float sc, uint32
   }
 }
 
+// Magnitude of x if it is finite, else 0: the FP16x3 scale follows the
+// operand's finite elements, so an infinity (which stays infinite under any
+// scale) does not leave the other elements unscaled and overflowing fp16.
+__device__ __forceinline__ float finite_abs(float x) {
+  const float a = fabsf(x);
+  return a <= FLT_MAX ? a : 0.f;  // false for inf and NaN
+}
+
 // Scale of an operand's FP16x3 pieces (1 for bf16 pieces).
 __device__ __forceinline__ float f16_scale_of(const unsigned* fmax) {
   return fmax ? pow2f(f16_scale_exp(*fmax)) : 1.f;
@@ -587,11 +597,11 @@ __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restri
   split_tile<NP, F16>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile, fmax);
 }
 
-// Largest magnitude of an operand stored as R rows x Cc columns with leading
-// dimension ld (the maximum does not depend on which of them is k), folded
-// into *word with atomicMax on its IEEE pattern, which orders non-negative
-// floats like their values.  NaNs are skipped (fmaxf); an infinity makes the
-// FP16x3 scale 1.  Blocks walk (row, 4096-column chunk) items grid-stride and
+// Largest finite magnitude of an operand stored as R rows x Cc columns with
+// leading dimension ld (the maximum does not depend on which of them is k),
+// folded into *word with atomicMax on its IEEE pattern, which orders
+// non-negative floats like their values.  NaNs and infinities are skipped:
+// they propagate through the pieces whatever the scale.  Blocks walk (row, 4096-column chunk) items grid-stride and
 // fold once at the end.
 __global__ void __launch_bounds__(256) operand_max_kernel(const float* __restrict__ src,
                                                           long long ld, int R, int Cc,
@@ -611,14 +621,15 @@ __global__ void __launch_bounds__(256) operand_max_kernel(const float* __restric
         const int c = c0 + i * 1024 + threadIdx.x * 4;
         if (c + 3 < cend) {
           const float4 v = *reinterpret_cast<const float4*>(row + c);
-          m = fmaxf(m, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+          m = fmaxf(m, fmaxf(fmaxf(finite_abs(v.x), finite_abs(v.y)),
+                             fmaxf(finite_abs(v.z), finite_abs(v.w))));
         } else {
           for (int e = 0; e < 4; ++e)
-            if (c + e < cend) m = fmaxf(m, fabsf(row[c + e]));
+            if (c + e < cend) m = fmaxf(m, finite_abs(row[c + e]));
         }
       }
     } else {
-      for (int c = c0 + threadIdx.x; c < cend; c += 256) m = fmaxf(m, fabsf(row[c]));
+      for (int c = c0 + threadIdx.x; c < cend; c += 256) m = fmaxf(m, finite_abs(row[c]));
     }
   }
 #pragma unroll
@@ -857,7 +868,7 @@ __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int e = 0; e < 4; ++e) m = fmaxf(m, fabsf(raw.v[i][e]));
+      for (int e = 0; e < 4; ++e) m = fmaxf(m, finite_abs(raw.v[i][e]));
   }
   if (cur >= 0) fold();
 }
