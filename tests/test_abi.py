@@ -109,6 +109,17 @@ def test_workspace_query_is_host_only(lib):
     assert ug.workspace_bytes("N", "N", 64, 64, 63, 63, 64, "simt") > 0
 
 
+def test_fp16x3_workspace_has_two_pieces_and_scale_words(lib):
+    # two fp16 pieces per element, each operand followed by a 256-byte
+    # trailer that receives its largest magnitude
+    n = ug.workspace_bytes("N", "N", 1536, 1536, 512, 512, 1536, "fp16x3")
+    assert n == 2 * (2 * 1536 * 512 * 2 + 256)
+    assert n < ug.workspace_bytes("N", "N", 1536, 1536, 512, 512, 1536, "bf16x6")
+    # K rounds up to 32 (the 64-deep stages read the rest as TMA zero fill)
+    assert ug.workspace_bytes("T", "T", 1536, 1536, 33, 1536, 33, "fp16x3") == \
+        2 * (2 * 1536 * 64 * 2 + 256)
+
+
 def test_fast_division_constants_are_exact():
     """The implicit im2col gather divides pixel and tap indices by run-time
     constants with q = (umulhi(x, m) + x) >> s (internal.h FastDiv);
