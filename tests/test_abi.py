@@ -92,6 +92,21 @@ def test_argument_checks_need_no_gpu(lib):
     assert f(b"R", b"N", b"N", 0, 4, 4, 1.0, None, 4, None, 4, 0.0, None, 4, 0, None) == ug.OK
 
 
+def test_noalloc_refuses_forms_it_does_not_run(lib):
+    """The allocation-free entry point runs the bf16 split forms; the others
+    are refused before any device work (host-only check)."""
+    f = lib.ugemm_sgemm_dev_noalloc
+    f.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    for prec in (ug.PREC_SIMT, ug.PREC_FP16X3):
+        assert f(b"R", b"N", b"N", 4, 4, 4, 1.0, 16, 4, 16, 4, 0.0, 16, 4, prec, None) == \
+            ug.ERR_UNSUPPORTED
+        assert b"bf16 split forms" in lib.ugemm_last_error_message()
+
+
 def test_compat_requires_init(lib):
     assert lib.sgemm_cuda_status(b"N", b"N", 2, 2, 2, 1.0, None, None, 0.0, None) == ug.ERR_NOT_INIT
 

@@ -101,7 +101,8 @@ extern "C" UGEMM_API int ugemm_sgemm_dev_noalloc(char major, char transa, char t
   if (M < 0 || N < 0 || K < 0) return fail(UGEMM_ERR_ARG, "negative dimension");
   int form = precision == UGEMM_PREC_AUTO ? UGEMM_PREC_BF16X6 : precision;
   if (form != UGEMM_PREC_BF16X6 && form != UGEMM_PREC_BF16X9 && form != UGEMM_PREC_BF16X3)
-    return fail(UGEMM_ERR_UNSUPPORTED, "the allocation-free entry point runs the split forms only");
+    return fail(UGEMM_ERR_UNSUPPORTED,
+                "the allocation-free entry point runs the bf16 split forms only (BF16X6, BF16X9, BF16X3)");
   // column-major C = op(A) op(B)  <=>  row-major C^T = op(B)^T op(A)^T
   Gemm g = row ? Gemm{static_cast<char>(ta), static_cast<char>(tb), M, N, K, alpha, beta, A, lda,
                       B, ldb, C, ldc}
