@@ -31,9 +31,9 @@
 //   2. GEMM kernel, 10 warps:
 //        warp 0   TMA producer: one 3-D TMA per operand per stage brings all
 //                 pieces of a 32-deep k slice (64-byte swizzle) into a 3-4
-//                 stage ring (mbarrier full/empty pairs) -- for one GEMM of
-//                 two-piece operands a 64-deep slice (128-byte swizzle) into
-//                 a 2-3 stage ring, which halves the per-stage overhead;
+//                 stage ring (mbarrier full/empty pairs) -- for two-piece
+//                 operands a 64-deep slice (128-byte swizzle) into a 2-3
+//                 stage ring, which halves the per-stage overhead;
 //        warp 1   allocates TMEM (2 x BN columns: main + corrections) and,
 //                 from one thread, issues the tcgen05.mma stream;
 //        warps 2-9  epilogue: chunk drains, then alpha/beta and the store of
@@ -601,8 +601,8 @@ __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restri
 // leading dimension ld (the maximum does not depend on which of them is k),
 // folded into *word with atomicMax on its IEEE pattern, which orders
 // non-negative floats like their values.  NaNs and infinities are skipped:
-// they propagate through the pieces whatever the scale.  Blocks walk (row, 4096-column chunk) items grid-stride and
-// fold once at the end.
+// they propagate through the pieces whatever the scale.  Blocks walk
+// (row, 4096-column chunk) items grid-stride and fold once at the end.
 __global__ void __launch_bounds__(256) operand_max_kernel(const float* __restrict__ src,
                                                           long long ld, int R, int Cc,
                                                           unsigned* word) {
