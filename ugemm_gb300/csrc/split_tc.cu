@@ -1053,44 +1053,17 @@ void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long
 
 ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* dev_err,
                           cudaStream_t st) {
-  const int Kp = kp_of(g.K);
   if (split_scratch_bytes(g, p) > ws.bytes) return UGEMM_ERR_ARENA_TOO_SMALL;
-  auto* ap = static_cast<__nv_bfloat16*>(ws.ptr);
-  auto* bp = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(ws.ptr) +
-                                               split_operand_bytes(p.pieces, g.M, g.K));
+  // scratch: [A pieces | B pieces | wave-tail partial tiles and table]
+  uint8_t* ap = static_cast<uint8_t*>(ws.ptr);
+  uint8_t* bp = ap + split_operand_bytes(p.pieces, g.M, g.K);
+  uint8_t* tail_scratch = bp + split_operand_bytes(p.pieces, g.N, g.K);
   long long a_sr, a_sk, b_sr, b_sk;
   split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
-  if (p.f16) {
-    ugemm_status s = split_operand_launch(2, g.A, a_sr, a_sk, g.M, g.K, ap, st, true);
-    if (s == UGEMM_OK) s = split_operand_launch(2, g.B, b_sr, b_sk, g.N, g.K, bp, st, true);
-    if (s != UGEMM_OK) return s;
-  } else if (p.pieces == 3) {
-    launch_split<3>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
-    launch_split<3>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
-  } else {
-    launch_split<2>(g.A, a_sr, a_sk, g.M, g.K, Kp, ap, st);
-    launch_split<2>(g.B, b_sr, b_sk, g.N, g.K, Kp, bp, st);
-  }
-  CUtensorMap ta, tb;
-  if (!split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K, &ta, &tb))
-    return UGEMM_ERR_CUDA;
-  TcProblem P = split_problem(g, p.pieces, p.block_n, 0);
-  if (p.f16) {
-    P.fmax_a = split_fmax_word(ap, 2, g.M, g.K);
-    P.fmax_b = split_fmax_word(bp, 2, g.N, g.K);
-  }
-  const int total = P.tiles_m * P.tiles_n;
-  const int chunk =
-      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
-  // a partial last wave of tiles runs as two k slices (multi.cu)
-  const TailPlan tail = tail_plan(g, p);
-  ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
-                                     tail.use ? tail.main_tiles : total, chunk, 0, dev_err, st);
-  if (s != UGEMM_OK || !tail.use) return s;
-  return tail_launch(g, p, tail, ap, bp,
-                     static_cast<uint8_t*>(ws.ptr) + split_operand_bytes(p.pieces, g.M, g.K) +
-                         split_operand_bytes(p.pieces, g.N, g.K),
-                     dev_err, st);
+  ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st, p.f16);
+  if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st, p.f16);
+  if (s != UGEMM_OK) return s;
+  return split_gemm_on_pieces(g, p, ap, bp, tail_scratch, dev_err, st);
 }
 
 ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,
@@ -1190,6 +1163,7 @@ ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void*
   }
   const int chunk =
       split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
+  // a partial last wave of tiles runs as two k slices (multi.cu)
   const TailPlan tail = tail_scratch ? tail_plan(g, p) : TailPlan{};
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,
                                      tail.use ? tail.main_tiles : P.tiles_m * P.tiles_n, chunk, 0,
