@@ -52,3 +52,12 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setenv("RANK", "1")
     bench.run_reference(argparse.Namespace(steps=1, warmup=0, gpus=2))
     assert capsys.readouterr().out == ""
+
+
+def test_headline_is_the_fastest_split_form_at_simt_error_or_better():
+    ms = {"bf16x6": 3.9, "fp16x3": 2.5}
+    assert bench.pick_headline(ms, {"bf16x6": 2.4e-7, "fp16x3": 3.6e-7}, 1.6e-6) == "fp16x3"
+    # a faster form less accurate than SIMT does not count
+    assert bench.pick_headline(ms, {"bf16x6": 2.4e-7, "fp16x3": 2.0e-6}, 1.6e-6) == "bf16x6"
+    # none qualifies: the three-piece form is reported (and its error shows it)
+    assert bench.pick_headline(ms, {"bf16x6": 2e-6, "fp16x3": 3e-6}, 1.6e-6) == "bf16x6"
