@@ -51,8 +51,9 @@ typedef enum {
   UGEMM_PREC_BF16X6 = 2, /* 3 bf16 pieces per operand, 6 piece products (tcgen05) */
   UGEMM_PREC_BF16X9 = 3, /* 3 bf16 pieces per operand, all 9 piece products (tcgen05) */
   UGEMM_PREC_BF16X3 = 4, /* 2 bf16 pieces, 3 products: ~16-bit accuracy, for error studies */
-  UGEMM_PREC_FP16X3 = 5, /* 2 fp16 pieces of the operand scaled by a power of two, 3 products
-                            (tcgen05): 22-bit operands, half the MMAs of BF16X6 */
+  UGEMM_PREC_FP16X3 = 5, /* 2 fp16 pieces per element, every row of op(A) and column of op(B)
+                            scaled by its own power of two; 3 products (tcgen05): 22-bit
+                            operands, half the MMAs of BF16X6 */
 } ugemm_precision;
 
 /* ------------------------------------------------------------------ */
@@ -120,12 +121,16 @@ UGEMM_API int ugemm_sgemm_dev(char major, char transa, char transb, int M, int N
  * cudaMalloc, cudaFree or allocating routine.  The split pieces of A and B
  * live in a fixed 64 MiB array in the library's device memory, held by every
  * GPU that loads the library until the process exits; calls whose scratch
- * (6 * (M + N) * roundup(K, 32) bytes for the three-piece forms) exceeds it
- * return UGEMM_ERR_ARENA_TOO_SMALL.  The first call on a device looks up the
- * array's device address (with that device current); make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU (other streams or host threads) race on it.  Device pointers,
- * stream-ordered, same arguments as ugemm_sgemm_dev. */
+ * exceeds it return UGEMM_ERR_ARENA_TOO_SMALL.  The scratch of a call is
+ * exactly ugemm_workspace_bytes with the same arguments: about
+ * 6 * (M + N) * roundup(K, 32) bytes of pieces for the three-piece forms,
+ * plus, when the last wave of output tiles runs as the wave-tail launch, its
+ * partial tiles.  The first call on a device looks up the array's device
+ * address (with that device current); make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams or host threads) race on it.  A kernel wait that gives up is
+ * reported by ugemm_check.  Device pointers, stream-ordered, same arguments
+ * as ugemm_sgemm_dev. */
 UGEMM_API int ugemm_sgemm_dev_noalloc(char major, char transa, char transb, int M, int N, int K,
                                       float alpha, const float *A, int lda, const float *B,
                                       int ldb, float beta, float *C, int ldc, int precision,
@@ -160,6 +165,38 @@ UGEMM_API int ugemm_sgemm_backward(char transa, char transb, int M, int N, int K
                          int lddc, float beta_a, float *dA, int ldda, float beta_b, float *dB,
                          int lddb, int precision, void *stream);
 
+/* Report a kernel wait timeout of the device-pointer calls (no reference
+ * counterpart: the reference reports no device errors).  The calls above are
+ * stream-ordered and return before their kernels run, so a bounded wait that
+ * gives up (UGEMM_ERR_TIMEOUT on the host-pointer calls) cannot be returned
+ * by them; it is recorded in a per-device error word instead.  This call
+ * synchronises `stream`, reads the word of ugemm_sgemm_dev, _dev_ex,
+ * ugemm_sgemm_backward and ugemm_sgemm_dev_noalloc on the current device,
+ * clears it and returns UGEMM_ERR_TIMEOUT (with the code in the last-error
+ * message) if any of their kernels gave up since the last check, else
+ * UGEMM_OK.  A stale code never disturbs a later call: each call moves it
+ * aside before its own kernels run.  The word is per device, shared by all
+ * streams.  (Grouped plans have their own word: ugemm_grouped_check.) */
+UGEMM_API int ugemm_check(void *stream);
+
+/* Test hook for the error reporting above (no reference counterpart): writes
+ * `code` into an error word of the current device with a synchronous host
+ * copy, as a timed-out kernel wait would -- which 0: the device-pointer
+ * calls' word, 1: the allocation-free entry point's (after its first call
+ * on the device).  Launches nothing; for tests of ugemm_check only. */
+UGEMM_API int ugemm_debug_set_error_word(int which, int code);
+
+/* FP64 GEMM on the GPU, C = alpha*op(A)*op(B) + beta*C on device pointers
+ * (same argument meaning as ugemm_sgemm_dev, double precision, no precision
+ * argument).  The accuracy oracle of the FP32 forms at sizes the reference's
+ * FP64 CPU GEMMs (dgemm_cpu, ugemm.h:162; _dgemm_c, gemm_cpu.h:284;
+ * dgemm_avx, dgemm_avx.h:844) cannot reach in test time: one FP64 fused
+ * multiply-add chain over k per element, no emulation.  Not on the FP32
+ * product path. */
+UGEMM_API int ugemm_dgemm_oracle_dev(char major, char transa, char transb, int M, int N, int K,
+                                     double alpha, const double *A, int lda, const double *B,
+                                     int ldb, double beta, double *C, int ldc, void *stream);
+
 /* Device information: SM count and compute capability of the current device. */
 UGEMM_API int ugemm_device_info(int *sm_count, int *cc_major, int *cc_minor);
 
@@ -183,11 +220,19 @@ typedef struct {
   float slope;
 } ugemm_problem;
 
-/* Tile configuration of a grouped launch (chosen by ugemm_tune_grouped). */
+/* Tile configuration and schedule of a grouped launch (chosen by
+ * ugemm_tune_grouped; all zero = the library's defaults). */
 typedef struct {
-  int block_n;  /* split form: CTA tile width 128 or 256; SIMT form: square tile 64 or 128 */
-  int chunk_k;  /* split form: k depth between main-accumulator drains (multiple of 32) */
-  int max_ctas; /* persistent CTAs; 0 = one per SM */
+  int block_n;   /* split form: CTA tile width 128 or 256; SIMT form: square tile 64 or 128 */
+  int chunk_k;   /* split form: k depth between main-accumulator drains (multiple of 32) */
+  int max_ctas;  /* persistent CTAs; 0 = one per SM */
+  int split_k;   /* split-K threshold: a problem whose tiles are longer than the launch's
+                    k-work / (split_k * CTAs) is cut into k slices of about that length;
+                    0 = 2, negative = never split */
+  int deal;      /* split form: tiles dealt to the persistent CTAs 0 = longest first to the
+                    least-loaded CTA, 1 = round robin */
+  int transpose; /* split form: 0 = compute C^T = op(B)^T op(A)^T where that wastes less of
+                    the 128-row tiles, 1 = never */
 } ugemm_tile_config;
 
 typedef struct ugemm_grouped_plan_s ugemm_grouped_plan;
@@ -212,12 +257,15 @@ UGEMM_API int ugemm_grouped_config(const ugemm_grouped_plan *plan, ugemm_tile_co
 UGEMM_API int ugemm_sgemm_grouped(int count, const ugemm_problem *problems, int precision,
                                   void *stream);
 
-/* Autotuner: time every candidate tile configuration of this problem set
- * and form on the current device (CUDA events, after warm-up), return the
- * fastest and remember it in the tuning cache (JSON lines at
- * $UGEMM_TUNE_CACHE, default ./ugemm_tune_cache.jsonl).  A cached entry is
- * returned without timing unless `force` is non-zero.  The problems' C
- * buffers are overwritten while timing. */
+/* Autotuner: time candidate configurations of this problem set and form on
+ * the current device (CUDA events, after warm-up; the best of three timed
+ * batches each) -- first the tile shape (block_n x chunk_k), then, one knob
+ * at a time from the best so far, the split-K threshold, the tile deal, the
+ * transposed tiles and the persistent grid size -- return the fastest and
+ * remember it in the tuning cache (JSON lines at $UGEMM_TUNE_CACHE, default
+ * ./ugemm_tune_cache.jsonl; each line also lists every candidate with its
+ * time).  A cached entry is returned without timing unless `force` is
+ * non-zero.  The problems' C buffers are overwritten while timing. */
 UGEMM_API int ugemm_tune_grouped(int count, const ugemm_problem *problems, int precision,
                                  int force, ugemm_tile_config *best, double *best_ms);
 
@@ -307,7 +355,8 @@ UGEMM_API int ugemm_sgemv(char trans, int M, int N, float alpha, const float *A,
  * kernel launch is bracketed by CUDA events on its own stream.  collect()
  * synchronises, returns the summed milliseconds and launch counts per kind
  * (0 SIMT GEMM, 1 split pre-pass, 2 split tcgen05 GEMM, 3 auxiliary, 4 grouped
- * GEMM) and clears the record. */
+ * GEMM, 5 control: the one-thread error-word fold that starts each
+ * device-pointer call) and clears the record. */
 UGEMM_API int ugemm_profile_enable(int on);
 UGEMM_API int ugemm_profile_collect(double *ms_per_kind, int *launches_per_kind, int nkinds);
 

@@ -18,6 +18,21 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running CPU test")
 
 
+@pytest.fixture(autouse=True)
+def no_silent_device_timeout(request):
+    """After every GPU test that used the library: no kernel wait of a
+    device-pointer call gave up unreported (ugemm_check raises if one did)."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    ug = sys.modules.get("ugemm_gb300")
+    if ug is None or ug._lib is None:
+        return
+    import torch
+    if torch.cuda.is_available():
+        ug.check()
+
+
 @pytest.fixture(scope="session")
 def golden():
     import numpy as np

@@ -125,14 +125,18 @@ def test_workspace_query_is_host_only(lib):
 
 
 def test_fp16x3_workspace_has_two_pieces_and_scale_words(lib):
-    # two fp16 pieces per element, each operand followed by a 256-byte
-    # trailer that receives its largest magnitude
+    # two fp16 pieces per element, each operand followed by a trailer of one
+    # word per row (rounded up to 256 bytes) that receives the row's largest
+    # magnitude, from which the row's scale follows
     n = ug.workspace_bytes("N", "N", 1536, 1536, 512, 512, 1536, "fp16x3")
-    assert n == 2 * (2 * 1536 * 512 * 2 + 256)
+    assert n == 2 * (2 * 1536 * 512 * 2 + 1536 * 4)
     assert n < ug.workspace_bytes("N", "N", 1536, 1536, 512, 512, 1536, "bf16x6")
     # K rounds up to 32 (the 64-deep stages read the rest as TMA zero fill)
     assert ug.workspace_bytes("T", "T", 1536, 1536, 33, 1536, 33, "fp16x3") == \
-        2 * (2 * 1536 * 64 * 2 + 256)
+        2 * (2 * 1536 * 64 * 2 + 1536 * 4)
+    # rows that are not a multiple of 64: the trailer rounds up to 256 bytes
+    assert ug.workspace_bytes("N", "N", 1000, 1000, 512, 512, 1000, "fp16x3") == \
+        2 * (2 * 1000 * 512 * 2 + 4096)
 
 
 def test_fast_division_constants_are_exact():

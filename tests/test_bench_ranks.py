@@ -61,3 +61,9 @@ def test_headline_is_the_fastest_split_form_at_simt_error_or_better():
     assert bench.pick_headline(ms, {"bf16x6": 2.4e-7, "fp16x3": 2.0e-6}, 1.6e-6) == "bf16x6"
     # none qualifies: the three-piece form is reported (and its error shows it)
     assert bench.pick_headline(ms, {"bf16x6": 2e-6, "fp16x3": 3e-6}, 1.6e-6) == "bf16x6"
+    # every measure counts: accurate normwise but worse in its worst row
+    simt = (1.6e-6, 2.0e-6, 1.5e-6)
+    assert bench.pick_headline(ms, {"bf16x6": (2.4e-7, 3e-7, 2e-7),
+                                    "fp16x3": (3.6e-7, 1.0, 3e-7)}, simt) == "bf16x6"
+    assert bench.pick_headline(ms, {"bf16x6": (2.4e-7, 3e-7, 2e-7),
+                                    "fp16x3": (3.6e-7, 5e-7, 3e-7)}, simt) == "fp16x3"

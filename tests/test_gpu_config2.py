@@ -1,9 +1,17 @@
 """North-star config 2: split-precision tensor-core SGEMM vs plain FP32 SIMT
 at 8192^3 and the ragged 4095 x 4097 x 1023, alpha = 1.5, beta = 0.5, all
-four transpose pairs, on U[-1,1) inputs and on a wide-range set (mantissa
-U[1,2), random sign, exponent uniform in [-8, 8]); normwise error of both
-forms against an FP64 GEMM on the GPU.  Both split forms (BF16x6 and FP16x3)
-must be at least as accurate as the FP32 SIMT form on every case."""
+four transpose pairs, on U[-1,1) inputs and on wide-range sets (mantissa
+U[1,2), random sign, exponent uniform in [-8, 8], and in [-40, 40]); error
+of every form against the GPU FP64 oracle (ugemm_dgemm_oracle_dev),
+normwise, in the worst row and in the worst column (which a form that loses
+whole rows or columns to a scale cannot pass).  Both split forms (BF16x6 and
+FP16x3) must be at least as accurate as the FP32 SIMT form in all three on
+every case but one: with exponents spread over [-40, 40] and k = 1023, each
+element of C is dominated by a few products, which SIMT's fused
+multiply-add computes exactly, while the split forms drop terms of about
+2^-24 of each product (BF16x6: a1b2 + a2b1; FP16x3 keeps 22 of 24 bits);
+there both stay within 2x of SIMT's error and below 1e-6 (measured 1.4-1.6x;
+at k = 8192 on the same set both are below SIMT)."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -24,10 +32,18 @@ def gpu():
 def draw(shape, kind, g):
     if kind == "uniform":
         return torch.rand(shape, device="cuda", generator=g) * 2 - 1
+    span = 8 if kind == "wide" else 40
     mant = 1 + torch.rand(shape, device="cuda", generator=g)
     sign = torch.where(torch.rand(shape, device="cuda", generator=g) < 0.5, -1.0, 1.0)
-    expo = torch.randint(-8, 9, shape, device="cuda", generator=g).float()
+    expo = torch.randint(-span, span + 1, shape, device="cuda", generator=g).float()
     return sign * mant * torch.exp2(expo)
+
+
+def rowwise(C, ref):
+    """max_i ||C_i - ref_i|| / ||ref_i|| and the same over columns."""
+    d = C.double() - ref
+    return (float((d.norm(dim=1) / ref.norm(dim=1)).max()),
+            float((d.norm(dim=0) / ref.norm(dim=0)).max()))
 
 
 def errors(ta, tb, M, N, K, kind, seed):
@@ -35,26 +51,31 @@ def errors(ta, tb, M, N, K, kind, seed):
     A = draw((M, K) if ta == "N" else (K, M), kind, g)
     B = draw((K, N) if tb == "N" else (N, K), kind, g)
     C0 = draw((M, N), kind, g)
-    ref = ALPHA * ((A.double() if ta == "N" else A.double().T) @
-                   (B.double() if tb == "N" else B.double().T)) + BETA * C0.double()
+    ref = ug.ref64(ta, tb, A, B, C0, ALPHA, BETA)
     out = {}
     for prec in ("simt", "bf16x6", "fp16x3"):
         C = C0.clone()
         ug.sgemm_dev(ta, tb, M, N, K, ALPHA, A, A.stride(0), B, B.stride(0), BETA, C, N,
                      precision=prec)
-        torch.cuda.synchronize()
-        out[prec] = float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref))
+        ug.check()
+        norm = float(torch.linalg.norm(C.double() - ref) / torch.linalg.norm(ref))
+        out[prec] = (norm, *rowwise(C, ref))
     return out
 
 
-@pytest.mark.parametrize("kind", ["uniform", "wide"])
+@pytest.mark.parametrize("kind", ["uniform", "wide", "wide40"])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
 @pytest.mark.parametrize("shape", [(8192, 8192, 8192), (4095, 4097, 1023)])
 def test_split_at_least_as_accurate_as_simt(shape, ta, tb, kind):
     M, N, K = shape
-    e = errors(ta, tb, M, N, K, kind, seed=M + 2 * N + 3 * K + ord(ta) + 5 * ord(tb))
-    print(f"{shape} {ta}{tb} {kind}: simt {e['simt']:.3e} bf16x6 {e['bf16x6']:.3e} "
-          f"fp16x3 {e['fp16x3']:.3e}")
-    assert e["bf16x6"] <= e["simt"], e
-    assert e["fp16x3"] <= e["simt"], e
-    assert e["simt"] < 1e-5
+    e = errors(ta, tb, M, N, K, kind, seed=M + 2 * N + 3 * K + ord(ta) + 5 * ord(tb) + len(kind))
+    print(f"{shape} {ta}{tb} {kind}: (normwise, worst row, worst column) " +
+          " ".join(f"{p} {v[0]:.2e}/{v[1]:.2e}/{v[2]:.2e}" for p, v in e.items()))
+    few_products = kind == "wide40" and K < 4096
+    for prec in ("bf16x6", "fp16x3"):
+        for i in range(3):
+            if few_products:
+                assert e[prec][i] <= 2 * e["simt"][i] and e[prec][i] < 1e-6, (prec, i, e)
+            else:
+                assert e[prec][i] <= e["simt"][i], (prec, i, e)
+    assert e["simt"][0] < 1e-5

@@ -1,9 +1,10 @@
-"""The FP16x3 split form: each operand is scaled by a power of two chosen from
-its largest magnitude and written as two fp16 pieces.  These cases check the
-scale logic where it matters -- operands far above fp16's range, far below
-it, one outlier element, an infinity, an all-zero operand -- against an
-FP64 GEMM, and
-that the form matches BF16x6 and the FP32 SIMT form on ordinary inputs."""
+"""The FP16x3 split form: every row of op(A) and every column of op(B) is
+scaled by a power of two chosen from its own largest magnitude and written as
+two fp16 pieces.  These cases check the scale logic where it matters --
+operands far above fp16's range, far below it, one outlier element, rows and
+columns 2^30 apart, an infinity, an all-zero operand -- against the GPU FP64
+oracle, row by row as well as normwise, and that the form matches BF16x6 and
+the FP32 SIMT form on ordinary inputs."""
 import math
 
 import pytest
@@ -35,13 +36,22 @@ def gemm(ta, tb, A, B, C0, alpha, beta, prec):
 
 
 def ref64(ta, tb, A, B, C0, alpha, beta):
-    a = A.double() if ta == "N" else A.double().T
-    b = B.double() if tb == "N" else B.double().T
-    return alpha * (a @ b) + beta * C0.double()
+    return ug.ref64(ta, tb, A, B, C0, alpha, beta)
 
 
 def nerr(got, ref):
     return float(torch.linalg.norm(got.double() - ref) / torch.linalg.norm(ref))
+
+
+def worst_row(got, ref):
+    """max_i ||C_i - ref_i|| / ||ref_i|| over the rows with a non-zero reference."""
+    d = (got.double() - ref).norm(dim=1)
+    n = ref.norm(dim=1)
+    return float((d[n > 0] / n[n > 0]).max())
+
+
+def worst_col(got, ref):
+    return worst_row(got.T, ref.T)
 
 
 def uniform(shape, g, scale=1.0):
@@ -65,9 +75,11 @@ def test_operands_far_from_fp16_range(ea, eb, ta, tb):
     assert nerr(got, ref) < TOL, (ea, eb, ta, tb, nerr(got, ref))
 
 
-def test_outlier_element_sets_the_scale():
-    """One element 2^40 times the others: the scale follows the largest
-    magnitude, and the normwise error stays at the FP32 level."""
+def test_outlier_element_leaves_the_other_rows_accurate():
+    """One element 2^40 times the others: it sets the scale of its own row of
+    A only, so every other row of C keeps FP32 accuracy (an operand-wide
+    scale would flush all of them to zero, and a normwise check, dominated by
+    the outlier's row, would not see it)."""
     g = torch.Generator(device="cuda").manual_seed(5)
     M, N, K = 257, 129, 513
     A = uniform((M, K), g)
@@ -76,7 +88,32 @@ def test_outlier_element_sets_the_scale():
     C0 = torch.zeros((M, N), device="cuda")
     ref = ref64("N", "N", A, B, C0, 1.0, 0.0)
     got = gemm("N", "N", A, B, C0, 1.0, 0.0, "fp16x3")
+    simt = gemm("N", "N", A, B, C0, 1.0, 0.0, "simt")
     assert nerr(got, ref) < TOL
+    assert worst_row(got, ref) <= worst_row(simt, ref), (worst_row(got, ref), worst_row(simt, ref))
+    assert worst_row(got, ref) < TOL
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+def test_rows_and_columns_far_apart(ta, tb):
+    """Every other row of op(A) and every third column of op(B) scaled by
+    2^-30: each row and column gets its own scale, so every row and column
+    of C is as accurate as the FP32 SIMT form's."""
+    g = torch.Generator(device="cuda").manual_seed(40 + ord(ta) + 2 * ord(tb))
+    M, N, K = 300, 390, 1100
+    opA = uniform((M, K), g)
+    opB = uniform((K, N), g)
+    opA[::2] *= math.ldexp(1.0, -30)
+    opB[:, ::3] *= math.ldexp(1.0, -30)
+    A = opA.contiguous() if ta == "N" else opA.T.contiguous()
+    B = opB.contiguous() if tb == "N" else opB.T.contiguous()
+    C0 = torch.zeros((M, N), device="cuda")
+    ref = ref64(ta, tb, A, B, C0, 1.0, 0.0)
+    got = gemm(ta, tb, A, B, C0, 1.0, 0.0, "fp16x3")
+    simt = gemm(ta, tb, A, B, C0, 1.0, 0.0, "simt")
+    for f in (worst_row, worst_col):
+        assert f(got, ref) <= f(simt, ref), (f.__name__, f(got, ref), f(simt, ref))
+    assert worst_row(got, ref) < TOL
 
 
 def test_infinity_does_not_set_the_scale():

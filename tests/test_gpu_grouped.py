@@ -161,7 +161,19 @@ def test_autotuner_caches_its_choice(tmp_path, monkeypatch):
     assert best["block_n"] in (128, 256) and best["chunk_k"] in (128, 256)
     assert ms > 0
     lines = [json.loads(x) for x in cache.read_text().splitlines()]
-    assert lines[-1]["block_n"] == best["block_n"]
+    line = lines[-1]
+    assert all(line[k] == v for k, v in best.items())
+    # every candidate is recorded with its time, the schedule knobs were
+    # searched (split-K threshold, tile deal, transposed tiles, grid size),
+    # and the choice is the fastest of them
+    cands = line["candidates"]
+    fields = ("block_n", "chunk_k", "max_ctas", "split_k", "deal", "transpose")
+    assert len(cands) >= 9
+    for i, name in enumerate(fields[2:], start=2):
+        assert len({c[i] for c in cands}) >= 2, name
+    fastest = min(cands, key=lambda c: c[6])
+    assert fastest[6] == pytest.approx(line["ms"], rel=1e-6)
+    assert dict(zip(fields, fastest[:6])) == best
     # cached: returned without timing, and picked up by a plan without config
     again, ms2 = ug.tune_grouped(specs, precision="bf16x6")
     assert again == best and ms2 == pytest.approx(ms, rel=1e-5)
@@ -173,3 +185,5 @@ def test_autotuner_caches_its_choice(tmp_path, monkeypatch):
     plan.close()
     simt_best, _ = ug.tune_grouped(specs, precision="simt", force=True)
     assert simt_best["block_n"] in (64, 128)
+    simt_line = json.loads(cache.read_text().splitlines()[-1])
+    assert min(c[6] for c in simt_line["candidates"]) == pytest.approx(simt_line["ms"], rel=1e-6)

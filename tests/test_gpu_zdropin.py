@@ -1,7 +1,9 @@
 """The drop-in seen from C: a C99 program that uses include/sgemm_cuda.h the
 way the reference's sgemm_test.c uses its OpenCL backend header compiles
 with -std=c99 -Wall -Werror, links against libugemm_cuda.so and runs (the
-host-only calls here; the known-answer GEMM too when a GPU is present)."""
+host-only calls here; with a GPU, the known-answer GEMM in an arena sized by
+the reference's own rule, 840 bytes for the 3 x 3 x 2 product, and a ragged
+product through each of sgemm_test.c's three transpose macros)."""
 import os
 import shutil
 import subprocess
@@ -22,7 +24,7 @@ def build_dropin(tmp_path):
     libdir = os.path.dirname(ug.LIB_PATH)
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "c", "dropin.c"), "-o", exe, "-L", libdir,
-                    "-lugemm_cuda", f"-Wl,-rpath,{libdir}"], check=True)
+                    "-lugemm_cuda", f"-Wl,-rpath,{libdir}", "-lm"], check=True)
     return exe
 
 

@@ -53,9 +53,10 @@ EXPORTS = (
     "ugemm_device_info", "ugemm_profile_enable", "ugemm_profile_collect",
     "ugemm_grouped_plan_create", "ugemm_grouped_run", "ugemm_grouped_check",
     "ugemm_grouped_plan_destroy", "ugemm_grouped_flops", "ugemm_grouped_config",
-    "ugemm_sgemm_grouped", "ugemm_tune_grouped",
+    "ugemm_sgemm_grouped", "ugemm_tune_grouped", "ugemm_check", "ugemm_dgemm_oracle_dev",
+    "ugemm_sgemm_dev_noalloc", "ugemm_debug_set_error_word",
 )
-PROF_KINDS = ("simt", "split_prepass", "split_gemm", "aux", "grouped")
+PROF_KINDS = ("simt", "split_prepass", "split_gemm", "aux", "grouped", "control")
 
 
 class UgemmError(RuntimeError):
@@ -121,6 +122,15 @@ def load() -> ctypes.CDLL:
     lib.ugemm_profile_enable.restype = _i
     lib.ugemm_profile_collect.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i), _i]
     lib.ugemm_profile_collect.restype = _i
+    lib.ugemm_check.argtypes = [_p]
+    lib.ugemm_check.restype = _i
+    lib.ugemm_debug_set_error_word.argtypes = [_i, _i]
+    lib.ugemm_debug_set_error_word.restype = _i
+    lib.ugemm_sgemm_dev_noalloc.argtypes = gemm + [_i, _p]
+    lib.ugemm_sgemm_dev_noalloc.restype = _i
+    d = ctypes.c_double
+    lib.ugemm_dgemm_oracle_dev.argtypes = [_c, _c, _c, _i, _i, _i, d, _p, _i, _p, _i, d, _p, _i, _p]
+    lib.ugemm_dgemm_oracle_dev.restype = _i
     _lib = lib
     return lib
 
@@ -196,6 +206,50 @@ def sgemm_dev(ta: str, tb: str, M: int, N: int, K: int, alpha: float, A, lda: in
     _check(lib.ugemm_sgemm_dev(major.encode(), ta.encode(), tb.encode(), M, N, K, alpha, ptr(A),
                                lda, ptr(B), ldb, beta, ptr(C), ldc, _prec(precision),
                                _stream_ptr(stream)))
+
+
+def sgemm_dev_noalloc(ta: str, tb: str, M: int, N: int, K: int, alpha: float, A, lda: int, B,
+                      ldb: int, beta: float, C, ldc: int, precision="bf16x6", stream=None,
+                      major: str = "R") -> None:
+    """ugemm_sgemm_dev_noalloc: the split forms with scratch in a fixed device array."""
+    lib = load()
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_sgemm_dev_noalloc(major.encode(), ta.encode(), tb.encode(), M, N, K, alpha,
+                                       ptr(A), lda, ptr(B), ldb, beta, ptr(C), ldc,
+                                       _prec(precision), _stream_ptr(stream)))
+
+
+def check(stream=None) -> None:
+    """ugemm_check: synchronise `stream`; raise UgemmError(ERR_TIMEOUT) if a kernel wait of
+    a device-pointer call gave up since the last check."""
+    _check(load().ugemm_check(_stream_ptr(stream)))
+
+
+def dgemm_oracle(ta: str, tb: str, M: int, N: int, K: int, alpha: float, A, lda: int, B,
+                 ldb: int, beta: float, C, ldc: int, stream=None, major: str = "R") -> None:
+    """ugemm_dgemm_oracle_dev: the FP64 GEMM the FP32 forms are checked against."""
+    lib = load()
+    ptr = (lambda t: t if isinstance(t, int) else t.data_ptr())
+    _check(lib.ugemm_dgemm_oracle_dev(major.encode(), ta.encode(), tb.encode(), M, N, K, alpha,
+                                      ptr(A), lda, ptr(B), ldb, beta, ptr(C), ldc,
+                                      _stream_ptr(stream)))
+
+
+def ref64(ta: str, tb: str, A, B, C0=None, alpha: float = 1.0, beta: float = 0.0):
+    """alpha*op(A)*op(B) + beta*C0 in FP64 on the device (float64 result) through
+    ugemm_dgemm_oracle_dev, from FP32 or FP64 row-major CUDA tensors."""
+    import torch
+    a, b = A.double().contiguous(), B.double().contiguous()
+    M = a.shape[0] if ta == "N" else a.shape[1]
+    K = a.shape[1] if ta == "N" else a.shape[0]
+    N = b.shape[1] if tb == "N" else b.shape[0]
+    if C0 is None or beta == 0.0:
+        C = torch.zeros((M, N), dtype=torch.float64, device=a.device)
+        beta = 0.0
+    else:
+        C = C0.double().contiguous().clone()
+    dgemm_oracle(ta, tb, M, N, K, alpha, a, a.shape[1], b, b.shape[1], beta, C, N)
+    return C
 
 
 def gemm(A, B, C=None, *, ta: str = "N", tb: str = "N", alpha: float = 1.0, beta: float = 0.0,
@@ -301,11 +355,12 @@ class Problem(ctypes.Structure):
 
 
 class TileConfig(ctypes.Structure):
-    """ugemm_tile_config."""
-    _fields_ = [("block_n", _i), ("chunk_k", _i), ("max_ctas", _i)]
+    """ugemm_tile_config: tile shape and schedule of a grouped launch."""
+    _fields_ = [("block_n", _i), ("chunk_k", _i), ("max_ctas", _i), ("split_k", _i),
+                ("deal", _i), ("transpose", _i)]
 
     def as_dict(self):
-        return {"block_n": self.block_n, "chunk_k": self.chunk_k, "max_ctas": self.max_ctas}
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 def _grouped_sigs(lib):

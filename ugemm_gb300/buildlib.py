@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libugemm_cuda.so")
 SOURCES = ["api.cu", "tmap.cu", "simt.cu", "split_tc.cu", "profile.cu", "grouped.cu", "tune.cu",
-           "conv.cu", "noalloc.cu", "pipeline.cu", "blas2.cu", "multi.cu", "selftest.cu"]
+           "conv.cu", "noalloc.cu", "pipeline.cu", "blas2.cu", "multi.cu", "selftest.cu", "dgemm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fvisibility=hidden"]

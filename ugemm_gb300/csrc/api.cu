@@ -25,7 +25,11 @@ thread_local std::string t_last_msg;
 
 struct DeviceState {
   bool ready = false;
-  int* dev_err = nullptr;     // device-side error word written by bounded waits
+  // Device-side error words: dev_err[0] is written by the bounded waits of
+  // the kernels of one call (the word the kernels see); dev_err[1] holds the
+  // first code that a device-pointer call left there, until ugemm_check
+  // reads it (error_fold_kernel moves it before the next call's kernels).
+  int* dev_err = nullptr;
   void* ws = nullptr;         // workspace of the device-pointer API
   size_t ws_bytes = 0;
   int sms = 0, cc_major = 0, cc_minor = 0;
@@ -74,14 +78,36 @@ ugemm_status device_state(DeviceState** out) {
     cudaDeviceGetAttribute(&d.cc_minor, cudaDevAttrComputeCapabilityMinor, dev);
     if (d.cc_major != 10 || d.cc_minor != 3)
       return fail(UGEMM_ERR_UNSUPPORTED, "libugemm_cuda is built for sm_103a (GB300)%s");
-    e = cudaMalloc(&d.dev_err, sizeof(int));
+    e = cudaMalloc(&d.dev_err, 2 * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(error word)");
-    e = cudaMemset(d.dev_err, 0, sizeof(int));
+    e = cudaMemset(d.dev_err, 0, 2 * sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(error word)");
     d.ready = true;
   }
   *out = &d;
   return UGEMM_OK;
+}
+
+// Stream-ordered start of a call on the device path: a code left in the
+// kernels' word by an earlier call moves to the held word (the first one is
+// kept) and the kernels' word is cleared, so a stale timeout neither stops
+// this call's waits early nor is reported as this call's; ugemm_check reports
+// it.  One thread, a few instructions.
+__global__ void error_fold_kernel(int* words) {
+  const int code = words[0];
+  if (code != 0) {
+    if (words[1] == 0) words[1] = code;
+    words[0] = 0;
+  }
+}
+
+ugemm_status begin_call(int* words, cudaStream_t st) {
+  (void)cudaGetLastError();  // a pending error of earlier, unrelated work is not this call's
+  prof_begin(st);
+  error_fold_kernel<<<1, 1, 0, st>>>(words);
+  prof_end(st, kProfControl);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? UGEMM_OK : cuda_fail(e, "error word fold");
 }
 
 bool is_capturing(cudaStream_t st) {
@@ -214,13 +240,70 @@ ugemm_status dev_gemm(const Gemm& g, int precision, cudaStream_t st) {
   const int form = resolve_form(precision, g);
   s = ensure_workspace(*d, scratch_for(g, form), st);
   if (s != UGEMM_OK) return s;
+  s = begin_call(d->dev_err, st);
+  if (s != UGEMM_OK) return s;
   return launch(g, form, Scratch{d->ws, d->ws_bytes}, d->dev_err, st);
+}
+
+// Host-pointer GEMM in an arena too small for the 256-byte-aligned layout:
+// A and B are packed into it with rows padded to 16 bytes (the host copies
+// do the padding, so the SIMT form needs no scratch: its tensor maps read the
+// packed rows directly), C tightly, regions 16-byte aligned, the scratch of a
+// split form 256-byte aligned after them.  The reference sizes its arena at
+// ten times the three matrices (sgemm_test.c:29), which this layout fits for
+// every shape in the SIMT form (at most 3 padding floats per row).
+ugemm_status host_gemm_tight(const Gemm& g, int form, void* arena, size_t arena_bytes,
+                             DeviceState& d, cudaStream_t st) {
+  const size_t a_rows = g.ta == 'N' ? g.M : g.K, b_rows = g.tb == 'N' ? g.K : g.N;
+  const size_t a_cols = g.ta == 'N' ? g.K : g.M, b_cols = g.tb == 'N' ? g.N : g.K;
+  const bool need_ab = g.K > 0 && g.alpha != 0.f;
+  const int lda4 = static_cast<int>(align_up(std::max<size_t>(a_cols, 1), 4));
+  const int ldb4 = static_cast<int>(align_up(std::max<size_t>(b_cols, 1), 4));
+  const size_t a_bytes = need_ab ? align_up(a_rows * lda4 * sizeof(float), 16) : 0;
+  const size_t b_bytes = need_ab ? align_up(b_rows * ldb4 * sizeof(float), 16) : 0;
+  const size_t c_bytes = size_t(g.M) * g.N * sizeof(float);
+  uint8_t* base = static_cast<uint8_t*>(arena);
+  Gemm dg = g;
+  dg.A = reinterpret_cast<const float*>(base);
+  dg.B = reinterpret_cast<const float*>(base + a_bytes);
+  dg.C = reinterpret_cast<float*>(base + a_bytes + b_bytes);
+  dg.lda = lda4;
+  dg.ldb = ldb4;
+  dg.ldc = g.N;
+  const size_t scratch = scratch_for(dg, form);
+  const size_t s_off = scratch ? align_up(a_bytes + b_bytes + c_bytes, 256) : a_bytes + b_bytes + c_bytes;
+  if (s_off + scratch > arena_bytes)
+    return fail(UGEMM_ERR_ARENA_TOO_SMALL, "device arena too small for this call%s");
+  cudaError_t e;
+  if (need_ab) {
+    e = cudaMemcpy2DAsync(const_cast<float*>(dg.A), lda4 * sizeof(float), g.A, g.lda * sizeof(float),
+                          a_cols * sizeof(float), a_rows, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy A to device");
+    e = cudaMemcpy2DAsync(const_cast<float*>(dg.B), ldb4 * sizeof(float), g.B, g.ldb * sizeof(float),
+                          b_cols * sizeof(float), b_rows, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy B to device");
+  }
+  if (g.beta != 0.f) {  // beta == 0: C is not read (sgemm_ocl2.h:177)
+    e = cudaMemcpy2DAsync(dg.C, g.N * sizeof(float), g.C, g.ldc * sizeof(float),
+                          g.N * sizeof(float), g.M, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "copy C to device");
+  }
+  ugemm_status s = launch(dg, form, Scratch{base + s_off, arena_bytes - s_off}, d.dev_err, st);
+  if (s != UGEMM_OK) return s;
+  e = cudaMemcpy2DAsync(g.C, g.ldc * sizeof(float), dg.C, g.N * sizeof(float), g.N * sizeof(float),
+                        g.M, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "copy C to host");
+  return check_device_error(d, st);
 }
 
 // Host-pointer GEMM through a device arena [A | B | C | scratch].
 ugemm_status host_gemm(const Gemm& g, int precision, void* arena, size_t arena_bytes,
                        DeviceState& d, cudaStream_t st) {
   if (g.M == 0 || g.N == 0) return UGEMM_OK;
+  {
+    ugemm_status bs = begin_call(d.dev_err, st);
+    if (bs != UGEMM_OK) return bs;
+  }
   const size_t a_rows = g.ta == 'N' ? g.M : g.K, b_rows = g.tb == 'N' ? g.K : g.N;
   const size_t a_cols = g.ta == 'N' ? g.K : g.M, b_cols = g.tb == 'N' ? g.N : g.K;
   const size_t a_bytes = align_up(a_rows * g.lda * sizeof(float), 256);
@@ -234,7 +317,7 @@ ugemm_status host_gemm(const Gemm& g, int precision, void* arena, size_t arena_b
   }
   const bool need_ab = g.K > 0 && g.alpha != 0.f;
   const size_t need = (need_ab ? a_bytes + b_bytes : 0) + c_bytes + scratch_for(g, form);
-  if (need > arena_bytes) return fail(UGEMM_ERR_ARENA_TOO_SMALL, "device arena too small for this call%s");
+  if (need > arena_bytes) return host_gemm_tight(g, form, arena, arena_bytes, d, st);
   uint8_t* base = static_cast<uint8_t*>(arena);
   Gemm dg = g;
   size_t off = 0;
@@ -503,6 +586,8 @@ int ugemm_sgemm_backward(char transa, char transb, int M, int N, int K, float al
       const SplitPlan p = split_plan_for(form, gs[0]);
       s = ensure_workspace(*d, multi_scratch_bytes(gs, n, p), st);
       if (s != UGEMM_OK) return s;
+      s = begin_call(d->dev_err, st);
+      if (s != UGEMM_OK) return s;
       s = multi_launch(gs, n, p, Scratch{d->ws, d->ws_bytes}, d->dev_err, st);
       if (s == UGEMM_ERR_CUDA) return cuda_fail(cudaGetLastError(), "kernel launch");
       if (s != UGEMM_OK) return fail(s, "launch failed%s");
@@ -530,6 +615,45 @@ int ugemm_sgemm_backward(char transa, char transb, int M, int N, int K, float al
     if (s != UGEMM_OK) return s;
   }
   return UGEMM_OK;
+}
+
+int ugemm_check(void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  std::lock_guard<std::mutex> lock(g_mu);
+  DeviceState* d = nullptr;
+  ugemm_status s = device_state(&d);
+  if (s != UGEMM_OK) return s;
+  int words[2] = {0, 0}, na[2] = {0, 0};
+  e = cudaMemcpy(words, d->dev_err, sizeof words, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(error words)");
+  int* nw = noalloc_error_words();
+  if (nw) {
+    e = cudaMemcpy(na, nw, sizeof na, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(error words)");
+  }
+  // the first recorded code wins: held codes are older than current ones
+  const int code = words[1] ? words[1] : words[0] ? words[0] : na[1] ? na[1] : na[0];
+  if (code == 0) return UGEMM_OK;
+  if (words[0] || words[1]) cudaMemset(d->dev_err, 0, sizeof words);
+  if (na[0] || na[1]) cudaMemset(nw, 0, sizeof na);
+  char buf[160];
+  std::snprintf(buf, sizeof buf,
+                "a kernel's pipeline wait timed out (code %d) in a device-pointer call", code);
+  set_last_error(UGEMM_ERR_TIMEOUT, buf);
+  return UGEMM_ERR_TIMEOUT;
+}
+
+int ugemm_debug_set_error_word(int which, int code) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  DeviceState* d = nullptr;
+  ugemm_status s = device_state(&d);
+  if (s != UGEMM_OK) return s;
+  int* word = which == 0 ? d->dev_err : which == 1 ? noalloc_error_words() : nullptr;
+  if (!word) return fail(UGEMM_ERR_ARG, "no such error word on this device (yet)%s");
+  const cudaError_t e = cudaMemcpy(word, &code, sizeof code, cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? UGEMM_OK : cuda_fail(e, "cudaMemcpy(error word)");
 }
 
 int ugemm_device_info(int* sm_count, int* cc_major, int* cc_minor) {

@@ -74,7 +74,8 @@ struct ugemm_grouped_plan_s {
   int nsub = 0;                   // kernel problems (split-K slices count one each)
   const void* reduce = nullptr;   // split-K reduce jobs
   const int4* tiles = nullptr;    // split form: per-CTA ranges, then one record per tile
-  unsigned* fmax = nullptr;       // FP16x3: the operands' largest magnitudes, two per problem
+  unsigned* fmax = nullptr;       // FP16x3: the largest magnitude of every operand row
+  int nfmax = 0;                  // words at fmax
   int grid = 0;                   // split form: persistent CTAs the tile table is dealt to
   int nreduce = 0;
   long long reduce_max = 0;       // largest M x N among them
@@ -109,7 +110,7 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
     return s == UGEMM_OK ? reduce_launch(p, st) : s;
   }
   s = split_batched_launch(p->split.pieces, static_cast<const SplitJob*>(p->jobs), p->njobs,
-                           p->prep_tiles, st, p->fmax, p->fmax ? 2 * p->count : 0);
+                           p->prep_tiles, st, p->fmax, p->nfmax);
   if (s != UGEMM_OK) return s;
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
@@ -261,7 +262,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
       o.tiles = cdiv(x.M, bn) * cdiv(x.N, bn);
       o.nkb = std::max(1, cdiv(x.K, kBK));
     } else {
-      o.swap = padded_area(x.N, x.M, bn) < padded_area(x.M, x.N, bn);
+      o.swap = p->cfg.transpose == 0 && padded_area(x.N, x.M, bn) < padded_area(x.M, x.N, bn);
       const int rows = o.swap ? x.N : x.M, cols = o.swap ? x.M : x.N;
       o.tiles = cdiv(rows, kTcBM) * cdiv(cols, bn);
       o.nkb = split_nkb(pieces, x.K);
@@ -277,7 +278,10 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   // (stages: 16 k-blocks of 32 in the SIMT form and the three-piece split
   // form, 8 of 64 for two-piece operands)
   const int min_slice = 16 * kTcKB / (simt ? kTcKB : split_stage_k(pieces));
-  const double fair = work / (2.0 * sms);
+  // (the threshold divisor is the configuration's split_k: 0 means 2,
+  // negative disables split-K)
+  const double fair = p->cfg.split_k < 0 ? 1e300
+                                          : work / ((p->cfg.split_k > 0 ? p->cfg.split_k : 2) * sms);
   std::vector<size_t> part_off(count, 0);
   size_t part_bytes = 0;
   for (int j = 0; j < count; ++j) {
@@ -456,29 +460,35 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   std::vector<int4> recs;
   if (!simt) {
     p->grid = std::max(1, std::min(tiles, p->cfg.max_ctas > 0 ? p->cfg.max_ctas : sms));
-    recs = split_tile_table(tprobs.data(), static_cast<int>(tprobs.size()), bn, p->grid);
+    recs = split_tile_table(tprobs.data(), static_cast<int>(tprobs.size()), bn, p->grid,
+                            p->cfg.deal == 1);
   }
   const size_t rec_bytes = recs.size() * sizeof(int4);
   const size_t off_t = off_r + align_up(std::max<size_t>(red_bytes, 1), 256);
-  // FP16x3: the operands' largest magnitudes, cleared on every run
+  // FP16x3: the largest magnitude of every row of every operand (job q's
+  // rows from word_off[q] on), cleared on every run
   const bool f16 = !simt && p->split.f16;
+  std::vector<size_t> word_off(sjobs.size() + 1, 0);
+  for (size_t q = 0; q < sjobs.size(); ++q) word_off[q + 1] = word_off[q] + sjobs[q].rows;
   const size_t off_w = off_t + align_up(std::max<size_t>(rec_bytes, 1), 256);
-  const size_t total = off_w + (f16 ? align_up(2 * size_t(count) * sizeof(unsigned), 256) : 0);
+  const size_t total =
+      off_w + (f16 ? align_up(std::max<size_t>(word_off.back(), 1) * sizeof(unsigned), 256) : 0);
   e = cudaMalloc(&p->table, total);
   if (e != cudaSuccess) {
     free_plan(p);
     return plan_fail(UGEMM_ERR_ALLOC, "grouped plan table allocation failed");
   }
   uint8_t* tb = static_cast<uint8_t*>(p->table);
-  if (f16) {  // operand j's word: jobs 2j (A) and 2j + 1 (B) fill it, its problems read it
+  if (f16) {  // problem j's row words: job 2j (A) and 2j + 1 (B) fill them, its slices read them
     unsigned* words = reinterpret_cast<unsigned*>(tb + off_w);
     p->fmax = words;
-    for (size_t q = 0; q < sjobs.size(); ++q) sjobs[q].fmax = words + q;
+    p->nfmax = static_cast<int>(word_off.back());
+    for (size_t q = 0; q < sjobs.size(); ++q) sjobs[q].fmax = words + word_off[q];
     for (size_t i = 0; i < tprobs.size(); ++i) {
       const int j = subs[i].j;
       const bool sw = geo[j].swap;  // kernel operand a is op(B)^T's pieces when swapped
-      tprobs[i].fmax_a = words + 2 * j + (sw ? 1 : 0);
-      tprobs[i].fmax_b = words + 2 * j + (sw ? 0 : 1);
+      tprobs[i].fmax_a = words + word_off[2 * j + (sw ? 1 : 0)];
+      tprobs[i].fmax_b = words + word_off[2 * j + (sw ? 0 : 1)];
     }
   }
   std::vector<uint8_t> host(total, 0);

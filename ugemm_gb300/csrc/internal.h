@@ -236,13 +236,18 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
 // Per-thread last error, shared by the void compat entry points.
 void set_last_error(ugemm_status s, const std::string& msg);
 
+// The allocation-free entry point's two error words on the current device
+// ([0] written by its kernels, [1] the code held for ugemm_check), or null
+// before its first call on the device.
+int* noalloc_error_words();
+
 }  // namespace ugemm
 
 namespace ugemm {
 // Optional per-kernel timing (CUDA events on the launching stream), enabled by
 // ugemm_profile_enable; used by the benchmark to attribute time to kernels.
 enum ProfKind : int { kProfSimt = 0, kProfSplitPrep = 1, kProfSplitGemm = 2, kProfAux = 3,
-                      kProfGrouped = 4, kProfKinds = 5 };
+                      kProfGrouped = 4, kProfControl = 5, kProfKinds = 6 };
 void prof_begin(cudaStream_t st);
 void prof_end(cudaStream_t st, int kind);
 }  // namespace ugemm

@@ -211,9 +211,9 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
     tp.tiles_m = cdiv(Mt, kTcBM);
     tp.tiles_n = cdiv(Nt, p.block_n);
     tp.tile_start = tiles;
-    if (p.f16) {  // the views share the whole operands' scales
-      tp.fmax_a = split_fmax_word(a_pieces, p.pieces, g.M, g.K);
-      tp.fmax_b = split_fmax_word(b_pieces, p.pieces, g.N, g.K);
+    if (p.f16) {  // the views' rows and columns keep the whole operands' scales
+      tp.fmax_a = split_fmax_word(a_pieces, p.pieces, g.M, g.K) + tail.r0;
+      tp.fmax_b = split_fmax_word(b_pieces, p.pieces, g.N, g.K) + tail.c0;
     }
     tiles += tp.tiles_m * tp.tiles_n;
   }

@@ -18,6 +18,10 @@
 // kernel, because on the host it names a host-side stand-in, not device
 // memory.  Calls share the array: two calls whose kernels overlap on the GPU
 // (different streams, or different host threads) race on it.
+//
+// A kernel wait that times out writes a code into this file's error word;
+// the next call moves it aside before its own kernels run (so it does not
+// stop them early) and ugemm_check reports it.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -33,7 +37,18 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-static __device__ __align__(16) int g_noalloc_err;
+// [0]: written by the kernels of a call; [1]: the first code an earlier call
+// left, held for ugemm_check
+static __device__ __align__(16) int g_noalloc_err[2];
+
+// Before a call's kernels: move a code an earlier call left to the held word.
+__global__ void noalloc_error_fold_kernel() {
+  const int code = g_noalloc_err[0];
+  if (code != 0) {
+    if (g_noalloc_err[1] == 0) g_noalloc_err[1] = code;
+    g_noalloc_err[0] = 0;
+  }
+}
 
 struct DeviceSlot {
   bool ready = false;
@@ -86,6 +101,14 @@ ugemm_status slot_for_current_device(DeviceSlot** out) {
 }
 
 }  // namespace
+
+int* noalloc_error_words() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lock(g_mu);
+  return g_slots[dev].ready ? g_slots[dev].err : nullptr;
+}
+
 }  // namespace ugemm
 
 using namespace ugemm;
@@ -95,7 +118,7 @@ extern "C" UGEMM_API int ugemm_sgemm_dev_noalloc(char major, char transa, char t
                                                  int lda, const float* B, int ldb, float beta,
                                                  float* C, int ldc, int precision, void* stream) {
   const int ta = trans_of(transa), tb = trans_of(transb);
-  if (!ta || !tb) return fail(UGEMM_ERR_ARG, "transpose flags must be 'N' or 'T'");
+  if (!ta || !tb) return fail(UGEMM_ERR_ARG, "transpose flags must be 'N', 'T' or 'C'");
   const bool row = (major == 'R' || major == 'r');
   if (!row && major != 'C' && major != 'c') return fail(UGEMM_ERR_ARG, "major must be 'R' or 'C'");
   if (M < 0 || N < 0 || K < 0) return fail(UGEMM_ERR_ARG, "negative dimension");
@@ -132,8 +155,13 @@ extern "C" UGEMM_API int ugemm_sgemm_dev_noalloc(char major, char transa, char t
                   need, kNoAllocScratchBytes);
     return fail(UGEMM_ERR_ARENA_TOO_SMALL, msg);
   }
-  // The error word is the only state a call reads: clear it before the launch.
-  cudaError_t e = cudaMemsetAsync(slot->err, 0, sizeof(int), st);
+  // A pending error of earlier, unrelated work is not this call's; a code an
+  // earlier call left in the error word is moved aside for ugemm_check.
+  (void)cudaGetLastError();
+  prof_begin(st);
+  noalloc_error_fold_kernel<<<1, 1, 0, st>>>();
+  prof_end(st, kProfControl);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(UGEMM_ERR_CUDA, cudaGetErrorString(e));
   s = split_launch(g, plan, Scratch{slot->scratch, kNoAllocScratchBytes}, slot->err, st);
   if (s != UGEMM_OK) {

@@ -328,12 +328,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmem_empty[buf]);
-      if constexpr (NP == 2) {  // FP16x3: undo the operands' power-of-two scales
+      if constexpr (NP == 2) {  // FP16x3: undo the rows' and columns' power-of-two scales
         if (P.fmax_a != nullptr) {
-          float s1, s2;
-          f16_unscale(*P.fmax_a, *P.fmax_b, s1, s2);
+          // this lane's row; lane l fetches the scales of columns l, l + 32, ...
+          // of the warp's half and hands them to the other lanes by shuffle
+          const int row = tc.m0 + q * 32 + lane;
+          const int ea = row < P.M ? f16_scale_exp(P.fmax_a[row]) : 0;
+          int eb[HALF / 32];
 #pragma unroll
-          for (int j = 0; j < HALF; ++j) acc[j] = acc[j] * s1 * s2;
+          for (int c32 = 0; c32 < HALF / 32; ++c32) {
+            const int col = tc.n0 + col_off + c32 * 32 + lane;
+            eb[c32] = col < P.N ? f16_scale_exp(P.fmax_b[col]) : 0;
+          }
+#pragma unroll
+          for (int j = 0; j < HALF; ++j)
+            acc[j] = scale_pow2(acc[j], -(ea + __shfl_sync(0xffffffffu, eb[j / 32], j % 32)));
         }
       }
       // alpha/beta epilogue (C not read when beta == 0).  The bias /
@@ -478,12 +487,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // ---------------------------------------------------------------- split pass
 // Pieces of two consecutive k of one row, each piece plane as one packed
 // 16-bit pair: bf16 pieces (x0 = bf16(x), x1 = bf16(x - x0), ...) or, with
-// F16, the FP16x3 form's two fp16 pieces of x * sc (sc = 2^e from
+// F16, the FP16x3 form's two fp16 pieces of x * 2^e (e = the row's
 // f16_scale_exp; only two-piece operands use it).
 template <int NP, bool F16>
-__device__ __forceinline__ void pieces_pair(float x0, float x1, float sc, uint32_t (&out)[NP]) {
+__device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t (&out)[NP]) {
   if constexpr (F16) {
-    const float y0 = x0 * sc, y1 = x1 * sc;
+    const float y0 = scale_pow2(x0, e), y1 = scale_pow2(x1, e);
     const __half h00 = __float2half_rn(y0), h01 = __float2half_rn(y1);
     const __half2 hi = __halves2half2(h00, h01);
     const __half2 lo = __halves2half2(__float2half_rn(y0 - __half2float(h00)),
@@ -513,9 +522,9 @@ __device__ __forceinline__ float finite_abs(float x) {
   return a <= FLT_MAX ? a : 0.f;  // false for inf and NaN
 }
 
-// Scale of an operand's FP16x3 pieces (1 for bf16 pieces).
-__device__ __forceinline__ float f16_scale_of(const unsigned* fmax) {
-  return fmax ? pow2f(f16_scale_exp(*fmax)) : 1.f;
+// Scale exponent of row r of an operand's FP16x3 pieces (0 for bf16 pieces).
+__device__ __forceinline__ int f16_row_exp(const unsigned* fmax, int r) {
+  return fmax ? f16_scale_exp(fmax[r]) : 0;
 }
 
 // One 32-row x 64-k tile of op(X) (element (r, k) at src[r*sr + k*sk]) into
@@ -570,12 +579,12 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ src, long l
   const int r = r0 + rr, k = k0 + g8;
   if (r < rows && k < Kp) {
     const size_t plane = static_cast<size_t>(rows) * Kp;
-    const float sc = F16 ? f16_scale_of(fmax) : 1.f;
+    const int ex = F16 ? f16_row_exp(fmax, r) : 0;
     uint32_t packed[NP][4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
       uint32_t two[NP];
-      pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], sc, two);
+      pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], ex, two);
 #pragma unroll
       for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
     }
@@ -595,53 +604,6 @@ __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restri
                                                            const unsigned* fmax) {
   __shared__ float tile[32][65];
   split_tile<NP, F16>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile, fmax);
-}
-
-// Largest finite magnitude of an operand stored as R rows x Cc columns with
-// leading dimension ld (the maximum does not depend on which of them is k),
-// folded into *word with atomicMax on its IEEE pattern, which orders
-// non-negative floats like their values.  NaNs and infinities are skipped:
-// they propagate through the pieces whatever the scale.  Blocks walk
-// (row, 4096-column chunk) items grid-stride and fold once at the end.
-__global__ void __launch_bounds__(256) operand_max_kernel(const float* __restrict__ src,
-                                                          long long ld, int R, int Cc,
-                                                          unsigned* word) {
-  const int chunks = (Cc + 4095) / 4096;
-  const long long items = static_cast<long long>(R) * chunks;
-  const bool vec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) && ((ld & 3) == 0);
-  float m = 0.f;
-  for (long long it = blockIdx.x; it < items; it += gridDim.x) {
-    const long long r = it / chunks;
-    const int c0 = static_cast<int>(it - r * chunks) * 4096;
-    const int cend = min(Cc, c0 + 4096);
-    const float* row = src + r * ld;
-    if (vec) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int c = c0 + i * 1024 + threadIdx.x * 4;
-        if (c + 3 < cend) {
-          const float4 v = *reinterpret_cast<const float4*>(row + c);
-          m = fmaxf(m, fmaxf(fmaxf(finite_abs(v.x), finite_abs(v.y)),
-                             fmaxf(finite_abs(v.z), finite_abs(v.w))));
-        } else {
-          for (int e = 0; e < 4; ++e)
-            if (c + e < cend) m = fmaxf(m, finite_abs(row[c + e]));
-        }
-      }
-    } else {
-      for (int c = c0 + threadIdx.x; c < cend; c += 256) m = fmaxf(m, finite_abs(row[c]));
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ float warp_max[8];
-  if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float b = warp_max[0];
-    for (int w = 1; w < 8; ++w) b = fmaxf(b, warp_max[w]);
-    if (b > 0.f) atomicMax(word, __float_as_uint(b));
-  }
 }
 
 // Raw values of one 32 x 64 tile, read with the same float4 pattern as
@@ -751,12 +713,12 @@ __device__ __forceinline__ void split_store(const SplitJob& j, int r0, int k0, f
   const int r = r0 + rr, k = k0 + g8;
   if (r >= j.rows || k >= j.Kp) return;
   const size_t plane = static_cast<size_t>(j.rows) * j.Kp;
-  const float sc = F16 ? f16_scale_of(j.fmax) : 1.f;
+  const int ex = F16 ? f16_row_exp(j.fmax, r) : 0;
   uint32_t packed[NP][4];
 #pragma unroll
   for (int e = 0; e < 8; e += 2) {
     uint32_t two[NP];
-    pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], sc, two);
+    pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], ex, two);
 #pragma unroll
     for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
   }
@@ -824,53 +786,117 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
   }
 }
 
-// FP16x3 form of the batched pre-pass, first step: the largest magnitude of
-// every job's operand (the same 32 x 64 tiles and loads as the split,
-// implicit im2col gathers included) folded into its `fmax` word.  A block
-// keeps a running maximum while its tiles belong to one job and folds it
-// with one atomicMax when the job changes, so a large operand costs one
-// atomic per block, not one per tile.
+// FP16x3 form, first step of the split: the largest finite magnitude of
+// every row of op(X), folded into the job's row words (j.fmax[r]) with
+// atomicMax on the IEEE pattern, which orders non-negative floats like their
+// values.  A tile (32 rows x 64 k, loaded as the split loads it, implicit
+// im2col gathers included) goes through shared memory so that both source
+// layouts reduce the same way: 8 threads per row, 8 values each, then a
+// shuffle reduction and one atomicMax per row and tile.  NaNs and infinities
+// are skipped: they propagate through the pieces whatever the scale.
+__device__ __forceinline__ void tile_row_max(const SplitJob& j, int r0, int k0, float (*tile)[65]) {
+  RawTile raw;
+  load_raw(j, r0, k0, raw);
+  raw_to_smem(j, raw, tile);
+  __syncthreads();
+  const int t = threadIdx.x, rr = t >> 3, g8 = (t & 7) * 8;
+  float m = 0.f;
+#pragma unroll
+  for (int e = 0; e < 8; ++e) m = fmaxf(m, finite_abs(tile[rr][g8 + e]));
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((t & 7) == 0 && r0 + rr < j.rows && m > 0.f) atomicMax(j.fmax + r0 + rr, __float_as_uint(m));
+  __syncthreads();
+}
+
+// One operand stored as a plain strided matrix, read once at full width
+// with nothing staged in shared memory until the end: element (r, k) at
+// src[r*sr + k*sk].  KCONTIG (sk == 1): 16 threads per row walk its k range
+// with float4 loads, 16 rows per block; otherwise (sr == 1: rows are
+// consecutive in memory) a thread keeps the maxima of 4 consecutive rows
+// (one float4 per k) and 4 threads share a k range, 256 rows per block.
+// Block (x, y) takes row band x and the y-th run of `kper` k; a shuffle or
+// shared-memory reduction ends with one atomicMax per row and block.
+template <bool KCONTIG, bool VEC>
+__global__ void __launch_bounds__(256) operand_row_max_kernel(const float* __restrict__ src,
+                                                              long long sr, long long sk, int rows,
+                                                              int K, int kper, unsigned* words) {
+  const int t = threadIdx.x;
+  const int k0 = blockIdx.y * kper, k1 = min(K, k0 + kper);
+  if constexpr (KCONTIG) {
+    const int r = blockIdx.x * 16 + (t >> 4), l = t & 15;
+    float m = 0.f;
+    if (r < rows) {
+      const float* row = src + r * sr;
+      if (VEC) {  // k0 and kper are multiples of 4 here
+        for (int k = k0 + 4 * l; k < k1; k += 64) {
+          if (k + 3 < k1) {
+            const float4 v = *reinterpret_cast<const float4*>(row + k);
+            m = fmaxf(m, fmaxf(fmaxf(finite_abs(v.x), finite_abs(v.y)),
+                               fmaxf(finite_abs(v.z), finite_abs(v.w))));
+          } else {
+            for (int e = k; e < k1; ++e) m = fmaxf(m, finite_abs(row[e]));
+          }
+        }
+      } else {
+        for (int k = k0 + l; k < k1; k += 16) m = fmaxf(m, finite_abs(row[k]));
+      }
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (l == 0 && r < rows && m > 0.f) atomicMax(words + r, __float_as_uint(m));
+  } else {
+    __shared__ float part[4][256];
+    const int q = t & 63, ty = t >> 6, r0 = blockIdx.x * 256 + 4 * q;
+    float m[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k = k0 + ty; k < k1; k += 4) {
+      const float* p = src + k * sk + r0;
+      if (VEC && r0 + 3 < rows) {
+        const float4 v = *reinterpret_cast<const float4*>(p);
+        m[0] = fmaxf(m[0], finite_abs(v.x));
+        m[1] = fmaxf(m[1], finite_abs(v.y));
+        m[2] = fmaxf(m[2], finite_abs(v.z));
+        m[3] = fmaxf(m[3], finite_abs(v.w));
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (r0 + e < rows) m[e] = fmaxf(m[e], finite_abs(p[e]));
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) part[ty][4 * q + e] = m[e];
+    __syncthreads();
+    const int r = blockIdx.x * 256 + t;
+    const float v = fmaxf(fmaxf(part[0][t], part[1][t]), fmaxf(part[2][t], part[3][t]));
+    if (r < rows && v > 0.f) atomicMax(words + r, __float_as_uint(v));
+  }
+}
+
+// One operand of any strides through the tiled reduction, tiles grid-stride.
+__global__ void __launch_bounds__(256) operand_max_single_kernel(const __grid_constant__ SplitJob j,
+                                                                 int total_tiles) {
+  __shared__ float tile[32][65];
+  for (int b = blockIdx.x; b < total_tiles; b += gridDim.x) {
+    int r0, k0;
+    tile_origin(j, b, r0, k0);
+    tile_row_max(j, r0, k0, tile);
+  }
+}
+
+// Many operands (grouped plans): blocks walk all jobs' tiles grid-stride.
 __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob* __restrict__ jobs,
                                                                   int njobs, int total_tiles) {
+  __shared__ float tile[32][65];
   __shared__ int starts[kJobCache];
-  __shared__ float warp_max[8];
   const int cached = min(njobs, kJobCache);
   for (int i = threadIdx.x; i < cached; i += blockDim.x) starts[i] = jobs[i].tile_start;
   __syncthreads();
-  float m = 0.f;
-  int cur = -1;
-  unsigned* word = nullptr;
-  auto fold = [&]() {  // every thread of the block, between tiles
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      float v = warp_max[0];
-      for (int w = 1; w < 8; ++w) v = fmaxf(v, warp_max[w]);
-      if (v > 0.f) atomicMax(word, __float_as_uint(v));
-    }
-    __syncthreads();
-    m = 0.f;
-  };
   for (int b = blockIdx.x; b < total_tiles; b += gridDim.x) {
-    const int ji = find_job(starts, jobs, njobs, b);
-    if (ji != cur) {
-      if (cur >= 0) fold();
-      cur = ji;
-      word = jobs[ji].fmax;
-    }
-    const SplitJob j = jobs[ji];
+    const SplitJob j = jobs[find_job(starts, jobs, njobs, b)];
     int r0, k0;
     tile_origin(j, b, r0, k0);
-    RawTile raw;
-    load_raw(j, r0, k0, raw);
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) m = fmaxf(m, finite_abs(raw.v[i][e]));
+    tile_row_max(j, r0, k0, tile);
   }
-  if (cur >= 0) fold();
 }
 
 template <int NP>
@@ -921,7 +947,8 @@ int kp_of(int K) { return static_cast<int>(align_up(std::max(K, 1), kTcKB)); }
 
 }  // namespace
 
-std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid) {
+std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid,
+                                   bool round_robin) {
   std::vector<int4> rec;
   std::vector<int> cost;
   for (int p = 0; p < nprob; ++p) {
@@ -941,16 +968,20 @@ std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_
   // 256-wide tiles: 135.5 us against 141.3 us dealt round robin)
   std::vector<int> order(rec.size());
   for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int>(i);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  using Load = std::pair<long long, int>;
-  std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
-  for (int c = 0; c < grid; ++c) heap.push({0, c});
   std::vector<std::vector<int>> lists(grid);
-  for (int i : order) {
-    const Load l = heap.top();
-    heap.pop();
-    lists[l.second].push_back(i);
-    heap.push({l.first + cost[i], l.second});
+  if (round_robin) {
+    for (int i : order) lists[i % grid].push_back(i);
+  } else {
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    using Load = std::pair<long long, int>;
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int c = 0; c < grid; ++c) heap.push({0, c});
+    for (int i : order) {
+      const Load l = heap.top();
+      heap.pop();
+      lists[l.second].push_back(i);
+      heap.push({l.first + cost[i], l.second});
+    }
   }
   std::vector<int4> table(grid + rec.size());
   int next = 0;
@@ -985,7 +1016,8 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
 }
 
 size_t split_operand_bytes(int pieces, int rows, int K) {
-  return align_up(size_t(pieces) * rows * kp_of(K) * 2, 256) + (pieces == 2 ? 256 : 0);
+  return align_up(size_t(pieces) * rows * kp_of(K) * 2, 256) +
+         (pieces == 2 ? align_up(size_t(std::max(rows, 1)) * sizeof(unsigned), 256) : 0);
 }
 
 unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K) {
@@ -1094,7 +1126,7 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
                                   cudaStream_t st, unsigned* fmax_words, int nwords) {
   if (total_tiles <= 0) return UGEMM_OK;
   const int grid = std::min(total_tiles, sm_count() * 8);
-  if (fmax_words) {  // FP16x3: every job's largest magnitude first
+  if (fmax_words) {  // FP16x3: the largest magnitude of every job's rows first
     if (pieces != 2) return UGEMM_ERR_ARG;
     if (cudaMemsetAsync(fmax_words, 0, sizeof(unsigned) * nwords, st) != cudaSuccess)
       return UGEMM_ERR_CUDA;
@@ -1127,20 +1159,35 @@ ugemm_status split_operand_launch(int pieces, const float* src, long long sr, lo
   auto* d = static_cast<__nv_bfloat16*>(dst);
   if (f16) {
     if (pieces != 2) return UGEMM_ERR_ARG;
-    unsigned* word = split_fmax_word(dst, 2, rows, K);
-    if (cudaMemsetAsync(word, 0, sizeof(unsigned), st) != cudaSuccess) return UGEMM_ERR_CUDA;
+    unsigned* words = split_fmax_word(dst, 2, rows, K);
+    if (cudaMemsetAsync(words, 0, sizeof(unsigned) * std::max(rows, 1), st) != cudaSuccess)
+      return UGEMM_ERR_CUDA;
     if (rows > 0 && K > 0) {
-      // the stored matrix: rows x K (k contiguous) or K x rows
+      // row bands x runs of k, about eight blocks per SM
       const bool kcontig = sk == 1;
-      const int R = kcontig ? rows : K, Cc = kcontig ? K : rows;
-      const long long ld = kcontig ? sr : sk;
-      const long long items = static_cast<long long>(R) * ((Cc + 4095) / 4096);
-      const int grid = static_cast<int>(std::min<long long>(items, sm_count() * 8LL));
+      const long long other = kcontig ? sr : sk;
+      const bool vec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) && ((other & 3) == 0);
+      const int band = kcontig ? 16 : 256, bands = cdiv(rows, band);
+      const int want_y = std::max(1, std::min(cdiv(K, 256), cdiv(sm_count() * 8, bands)));
+      const int kper = static_cast<int>(align_up(cdiv(K, want_y), 64));
+      const dim3 grid(bands, cdiv(K, kper));
       prof_begin(st);
-      operand_max_kernel<<<grid, 256, 0, st>>>(src, ld, R, Cc, word);
+      if (kcontig) {
+        if (vec) operand_row_max_kernel<true, true><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, kper, words);
+        else operand_row_max_kernel<true, false><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, kper, words);
+      } else if (sr == 1) {
+        if (vec) operand_row_max_kernel<false, true><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, kper, words);
+        else operand_row_max_kernel<false, false><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, kper, words);
+      } else {  // neither layout contiguous (not produced by the callers): the tiled reduction
+        SplitJob j{src, sr, sk, d, rows, K, Kp, 0};
+        j.fmax = words;
+        const int tiles = cdiv(rows, 32) * cdiv(Kp, 64);
+        j.tile_start = 0;
+        operand_max_single_kernel<<<std::min(tiles, sm_count() * 8), 256, 0, st>>>(j, tiles);
+      }
       prof_end(st, kProfSplitPrep);
     }
-    launch_split<2>(src, sr, sk, rows, K, Kp, d, st, word);
+    launch_split<2>(src, sr, sk, rows, K, Kp, d, st, words);
   } else if (pieces == 3) {
     launch_split<3>(src, sr, sk, rows, K, Kp, d, st);
   } else {

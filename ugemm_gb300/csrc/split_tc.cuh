@@ -17,20 +17,24 @@ constexpr int kTcEpiWarps = 8;   // two per TMEM lane quarter
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
 constexpr int kTcRaster = 8;     // tile rows per raster group (L2 reuse)
 
-// FP16x3 form: each FP32 operand is scaled by a power of two 2^e, chosen from
-// its largest magnitude m so that m * 2^e lies in [2^14, 2^15), and written
-// as two fp16 pieces h0 = fp16(x 2^e), h1 = fp16(x 2^e - h0) (11 + 11
-// significand bits; the rest, < 2^-22 |x| 2^e, is dropped with the h1*g1
-// product).  The scale keeps fp16 from overflowing (largest 65504) and keeps
-// both pieces of the large elements normal (h1 >= 2^-14), so the products
-// carry 22 bits of every element that matters in the normwise sense.  `bits`
-// is the IEEE pattern of m; the exponent is clamped so that 2^e and 2^-e are
-// normal floats (all-zero or non-finite operands get e = 0).
+// FP16x3 form: every row of an operand's K-major piece matrix -- a row of
+// op(A), a column of op(B) -- is scaled by its own power of two 2^e, chosen
+// from that row's largest magnitude m so that m * 2^e lies in [2^14, 2^15),
+// and written as two fp16 pieces h0 = fp16(x 2^e), h1 = fp16(x 2^e - h0)
+// (11 + 11 significand bits; the rest, < 2^-22 |x| 2^e, is dropped with the
+// h1*g1 product).  The scale keeps fp16 from overflowing (largest 65504) and
+// keeps both pieces of the row's large elements normal (h1 >= 2^-14); being
+// per row and per column, it follows rows and columns of very different
+// magnitudes, so one large element or one large row does not push the rest
+// of the operand below fp16's range.  C[i][j] is then the accumulator times
+// 2^-(eA[i] + eB[j]).  `bits` is the IEEE pattern of m (a row word written by
+// atomicMax); an all-zero or non-finite m gives e = 0.  e lies in
+// [-113, 163]: the largest finite float needs -113, the smallest subnormal
+// 163.
 __host__ __device__ __forceinline__ int f16_scale_exp(unsigned bits) {
   if (bits == 0u || bits >= 0x7F800000u) return 0;
   const int biased = static_cast<int>(bits >> 23);
-  const int e = 14 - (biased == 0 ? -127 : biased - 127);
-  return e < -113 ? -113 : (e > 126 ? 126 : e);
+  return 14 - (biased == 0 ? -127 : biased - 127);
 }
 // 2^e for -126 <= e <= 127, exactly.
 __host__ __device__ __forceinline__ float pow2f(int e) {
@@ -38,14 +42,17 @@ __host__ __device__ __forceinline__ float pow2f(int e) {
   v.u = static_cast<unsigned>(127 + e) << 23;
   return v.f;
 }
-// Factors s1 * s2 = 2^-(eA + eB) that undo both operands' scales, each a
-// normal float, applied one after the other so that the intermediate stays
-// between the accumulator's and the result's magnitudes.
-__host__ __device__ __forceinline__ void f16_unscale(unsigned a_bits, unsigned b_bits, float& s1,
-                                                     float& s2) {
-  const int e = f16_scale_exp(a_bits) + f16_scale_exp(b_bits), e1 = e / 2;
-  s1 = pow2f(-e1);
-  s2 = pow2f(-(e - e1));
+// x * 2^e.  One multiplication by a normal power of two when 2^e is one;
+// otherwise two, each by a normal power of two, splitting e in halves (|e|
+// is clamped to 252, beyond which any finite FP32 accumulator underflows to
+// zero or the operand scales could not produce it).  A multiplication by a
+// power of two is exact unless its result is subnormal, so scaling up is
+// exact and scaling down rounds only results that are subnormal anyway.
+__host__ __device__ __forceinline__ float scale_pow2(float x, int e) {
+  if (e >= -126 && e <= 127) return x * pow2f(e);
+  e = e < -252 ? -252 : (e > 252 ? 252 : e);
+  const int e1 = e / 2;
+  return (x * pow2f(e1)) * pow2f(e - e1);
 }
 
 // Tile `local` of a tiles_m x tiles_n GEMM: raster groups of kTcRaster tile
@@ -110,8 +117,10 @@ struct TcProblem {
   int swap = 0;
   int map = 0;          // tensor maps of this problem: maps[2 * map], maps[2 * map + 1]
   Epilogue epi;
-  // FP16x3 form: the largest magnitudes of the kernel's a and b operands
-  // (f16_scale_exp); the epilogue undoes their scales.  Null otherwise.
+  // FP16x3 form: the largest magnitude of every kernel row (fmax_a[r], a row
+  // of the kernel's a operand) and column (fmax_b[c], a row of its b
+  // operand), from which f16_scale_exp gives the scales the epilogue undoes.
+  // Null otherwise.
   const unsigned* fmax_a = nullptr;
   const unsigned* fmax_b = nullptr;
 };
@@ -127,8 +136,8 @@ struct SplitJob {
   // 2 = rows are taps and k pixels; 0 = plain strided matrix
   int gather = 0;
   Im2col im;
-  // FP16x3 form: the word that receives the operand's largest magnitude
-  // (operand_max_batched_kernel), from which the pieces' power-of-two scale
+  // FP16x3 form: `rows` words that receive the largest magnitude of each row
+  // (operand_max_batched_kernel), from which each row's power-of-two scale
   // follows; null: bf16 pieces.
   unsigned* fmax = nullptr;
 };
@@ -136,8 +145,8 @@ struct SplitJob {
 int split_kp(int K);
 int split_default_chunk_kb();
 // Bytes of one operand's pieces [pieces][rows][Kp]; two-piece operands also
-// carry a 256-byte trailer whose first word is the operand's largest
-// magnitude (split_fmax_word), used by the FP16x3 form.
+// carry a trailer of one word per row (rounded up to 256 bytes) that holds
+// the row's largest magnitude (split_fmax_word), used by the FP16x3 form.
 size_t split_operand_bytes(int pieces, int rows, int K);
 unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K);
 void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
@@ -187,16 +196,18 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
 // Tile table of a grouped launch of `grid` persistent CTAs: grid ranges
 // {first, end, 0, 0} into the records that follow, one {problem, m0, n0, 0}
 // per tile (raster order within a problem), dealt longest first to the
-// least-loaded CTA.
-std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid);
+// least-loaded CTA (round_robin: in problem order, tile i to CTA i % grid).
+std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_n, int grid,
+                                   bool round_robin = false);
 // The batched pre-pass of a grouped plan.  fmax_words (FP16x3 plans): the
-// jobs' `fmax` words, nwords of them contiguous, cleared and filled before
-// the split.
+// jobs' `fmax` row words, nwords of them contiguous, cleared and filled
+// before the split.
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st, unsigned* fmax_words = nullptr, int nwords = 0);
 // Split one operand into its pieces at dst (split_operand_bytes of room).
-// f16: FP16x3 pieces -- the largest magnitude is first found into the
-// operand's trailer word (cleared here), then the pieces are scaled by it.
+// f16: FP16x3 pieces -- the largest magnitude of every row is first found
+// into the operand's trailer words (cleared here), then each row's pieces
+// are scaled by its own.
 ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
                                   int rows, int K, void* dst, cudaStream_t st, bool f16 = false);
 // GEMM on operands already split; with tail_scratch (tail_scratch_bytes of

@@ -11,6 +11,7 @@
 #include <cinttypes>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -57,24 +58,27 @@ uint64_t signature(int count, const ugemm_problem* q, int form) {
   return h;
 }
 
+// One cache line: the chosen configuration and its time, then every
+// candidate timed as [block_n, chunk_k, max_ctas, split_k, deal, transpose, ms].
 bool lookup(const std::string& dev, int form, uint64_t sig, ugemm_tile_config* cfg, double* ms) {
   FILE* f = std::fopen(cache_path().c_str(), "r");
   if (!f) return false;
-  char line[512];
+  std::vector<char> line(1 << 16);
   bool found = false;
-  while (std::fgets(line, sizeof line, f)) {
+  while (std::fgets(line.data(), static_cast<int>(line.size()), f)) {
     char d[128];
-    int fm = 0, bn = 0, ck = 0, mc = 0;
+    int fm = 0;
+    ugemm_tile_config c{};
     uint64_t s = 0;
     double t = 0;
-    if (std::sscanf(line,
+    if (std::sscanf(line.data(),
                     "{\"device\": \"%127[^\"]\", \"form\": %d, \"sig\": \"%" SCNx64
-                    "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"ms\": %lf}",
-                    d, &fm, &s, &bn, &ck, &mc, &t) == 7 &&
+                    "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"split_k\": %d, "
+                    "\"deal\": %d, \"transpose\": %d, \"ms\": %lf",
+                    d, &fm, &s, &c.block_n, &c.chunk_k, &c.max_ctas, &c.split_k, &c.deal,
+                    &c.transpose, &t) == 10 &&
         dev == d && fm == form && s == sig) {
-      cfg->block_n = bn;
-      cfg->chunk_k = ck;
-      cfg->max_ctas = mc;
+      *cfg = c;
       if (ms) *ms = t;
       found = true;  // the last matching line wins
     }
@@ -83,13 +87,27 @@ bool lookup(const std::string& dev, int form, uint64_t sig, ugemm_tile_config* c
   return found;
 }
 
-void store(const std::string& dev, int form, uint64_t sig, const ugemm_tile_config& c, double ms) {
+struct Timed {
+  ugemm_tile_config c;
+  double ms;
+};
+
+void store(const std::string& dev, int form, uint64_t sig, const ugemm_tile_config& c, double ms,
+           const std::vector<Timed>& all) {
   FILE* f = std::fopen(cache_path().c_str(), "a");
   if (!f) return;
   std::fprintf(f,
                "{\"device\": \"%s\", \"form\": %d, \"sig\": \"%016" PRIx64
-               "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"ms\": %.6f}\n",
-               dev.c_str(), form, sig, c.block_n, c.chunk_k, c.max_ctas, ms);
+               "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"split_k\": %d, "
+               "\"deal\": %d, \"transpose\": %d, \"ms\": %.6f, \"candidates\": [",
+               dev.c_str(), form, sig, c.block_n, c.chunk_k, c.max_ctas, c.split_k, c.deal,
+               c.transpose, ms);
+  for (size_t i = 0; i < all.size(); ++i) {
+    const ugemm_tile_config& x = all[i].c;
+    std::fprintf(f, "%s[%d, %d, %d, %d, %d, %d, %.6f]", i ? ", " : "", x.block_n, x.chunk_k,
+                 x.max_ctas, x.split_k, x.deal, x.transpose, all[i].ms);
+  }
+  std::fprintf(f, "]}\n");
   std::fclose(f);
 }
 
@@ -120,49 +138,94 @@ UGEMM_API int ugemm_tune_grouped(int count, const ugemm_problem* problems, int p
     std::lock_guard<std::mutex> l(g_tmu);
     if (lookup(dev, form, sig, best, best_ms)) return UGEMM_OK;
   }
-  std::vector<ugemm_tile_config> cands;
-  if (form == UGEMM_PREC_SIMT) {
-    for (int bn : {64, 128}) cands.push_back(ugemm_tile_config{bn, 0, 0});
-  } else {
-    // chunk_k <= 256 keeps the split form at least as accurate as FP32 SIMT
-    for (int bn : {128, 256})
-      for (int ck : {128, 256}) cands.push_back(ugemm_tile_config{bn, ck, 0});
-  }
   cudaStream_t st;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return UGEMM_ERR_CUDA;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  double best_t = 1e30;
-  int rc = UGEMM_ERR_UNSUPPORTED;
-  for (const auto& c : cands) {
+  int sms = 148, dev_id = 0;
+  cudaGetDevice(&dev_id);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id);
+  std::vector<Timed> all;
+  // time one candidate (the best of three batches of five runs); < 0: failed
+  auto time_cfg = [&](const ugemm_tile_config& c) -> double {
+    for (const Timed& t : all)
+      if (std::memcmp(&t.c, &c, sizeof c) == 0) return t.ms;
     ugemm_grouped_plan* p = nullptr;
-    if (ugemm_grouped_plan_create(count, problems, form, &c, 0, &p) != UGEMM_OK) continue;
+    if (ugemm_grouped_plan_create(count, problems, form, &c, 0, &p) != UGEMM_OK) return -1.0;
     bool ok = true;
     for (int w = 0; w < 2 && ok; ++w) ok = ugemm_grouped_run(p, st) == UGEMM_OK;
-    const int reps = 5;
-    cudaEventRecord(e0, st);
-    for (int r = 0; r < reps && ok; ++r) ok = ugemm_grouped_run(p, st) == UGEMM_OK;
-    cudaEventRecord(e1, st);
+    double best = 1e30;
+    for (int batch = 0; batch < 3 && ok; ++batch) {
+      const int reps = 5;
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < reps && ok; ++r) ok = ugemm_grouped_run(p, st) == UGEMM_OK;
+      cudaEventRecord(e1, st);
+      ok = ok && cudaEventSynchronize(e1) == cudaSuccess;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best = std::min(best, double(ms) / reps);
+    }
     ok = ok && ugemm_grouped_check(p, st) == UGEMM_OK;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
     ugemm_grouped_plan_destroy(p);
-    if (!ok) continue;
-    const double t = ms / reps;
-    if (t < best_t) {
-      best_t = t;
-      *best = c;
-      rc = UGEMM_OK;
+    if (!ok) return -1.0;
+    all.push_back(Timed{c, best});
+    return best;
+  };
+  ugemm_tile_config cur{};
+  double cur_t = 1e30;
+  auto consider = [&](const ugemm_tile_config& c) {
+    const double t = time_cfg(c);
+    if (t >= 0 && t < cur_t) {
+      cur_t = t;
+      cur = c;
+    }
+  };
+  // 1. tile shape
+  if (form == UGEMM_PREC_SIMT) {
+    for (int bn : {64, 128}) consider(ugemm_tile_config{bn, 0, 0, 0, 0, 0});
+  } else {
+    // chunk_k <= 256 keeps the split form at least as accurate as FP32 SIMT
+    for (int bn : {128, 256})
+      for (int ck : {128, 256}) consider(ugemm_tile_config{bn, ck, 0, 0, 0, 0});
+  }
+  // 2. schedule, one knob at a time from the best so far
+  if (cur_t < 1e30) {
+    const ugemm_tile_config base = cur;
+    for (int sk : {1, 4, -1}) {
+      ugemm_tile_config c = base;
+      c.split_k = sk;
+      consider(c);
+    }
+    if (form != UGEMM_PREC_SIMT) {
+      ugemm_tile_config c = cur;
+      c.deal = 1;
+      consider(c);
+      c = cur;
+      c.transpose = 1;
+      consider(c);
+    }
+    for (int mc : {sms - sms / 8, sms / 2}) {
+      ugemm_tile_config c = cur;
+      c.max_ctas = mc;
+      consider(c);
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaStreamDestroy(st);
+  int rc = UGEMM_ERR_UNSUPPORTED;
+  double best_t = 1e30;
+  for (const Timed& t : all)  // the fastest of everything timed
+    if (t.ms < best_t) {
+      best_t = t.ms;
+      *best = t.c;
+      rc = UGEMM_OK;
+    }
   if (rc == UGEMM_OK) {
     if (best_ms) *best_ms = best_t;
     std::lock_guard<std::mutex> l(g_tmu);
-    store(dev, form, sig, *best, best_t);
+    store(dev, form, sig, *best, best_t, all);
   }
   return rc;
 }
