@@ -4,7 +4,7 @@ One step = one SGEMM C = 1.5*A*B + 0.5*C at M=N=K=8192, FP32 row-major, NN,
 inputs U[-1,1) (seeded, resident in HBM; each operand is 256 MiB, larger than
 the 129 MB L2, so no explicit flush between steps).  The headline `value` is
 the split-precision tensor-core form in TFLOPS (2*M*N*K per step): of the two
-split forms measured (BF16x6 and FP16x3 on tcgen05), the faster one whose
+split forms measured (BF16x6, FP16x3 and TF32x3 on tcgen05), the fastest one whose
 error against FP64 is at most the plain FP32 SIMT form's -- normwise and in
 its worst row, on the benchmark's inputs and on a 4096^3 problem whose
 exponents span [-40, 40] (worst row and worst column too).  The SIMT form,
@@ -450,7 +450,9 @@ def main():
         return (float(torch.linalg.norm(d) / torch.linalg.norm(ref)),
                 float((d.norm(dim=1) / ref.norm(dim=1)).max()))
 
-    split_forms = {"bf16x6": 6, "fp16x3": 3}  # piece products per FP32 product
+    # 16-bit-rate piece products per FP32 product (TF32 MMAs run at half the
+    # 16-bit dense rate: three TF32 products cost six)
+    split_forms = {"bf16x6": 6, "fp16x3": 3, "tf32x3": 6}
     errs_main = {prec: form_error(prec) for prec in list(split_forms) + ["simt"]}
     del ref
     torch.cuda.empty_cache()
@@ -505,19 +507,25 @@ def main():
     lib.sgemm_cuda_set_precision(ug.PRECISIONS[head])
     e2e_steps = max(2, args.steps // 2)
 
-    def e2e_call():
-        ug._check(lib.sgemm_cuda_status(b"N", b"N", M, N, K, alpha, hA.data_ptr(), hB.data_ptr(),
-                                        beta, hC.data_ptr()))
+    def e2e_time(a_ptr, b_ptr, c_ptr):
+        def call():
+            ug._check(lib.sgemm_cuda_status(b"N", b"N", M, N, K, alpha, a_ptr, b_ptr, beta, c_ptr))
+        for _ in range(2):
+            call()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            call()
+        return max_over_ranks((time.perf_counter() - t0) / e2e_steps, world,
+                              torch.device("cuda", local))
 
-    for _ in range(2):
-        e2e_call()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_call()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = e2e_time(hA.data_ptr(), hB.data_ptr(), hC.data_ptr())
+    # the reference's callers pass pageable memory (sgemm_test.c's static
+    # arrays): the same call on plain numpy arrays
+    nA, nB, nC = hA.numpy().copy(), hB.numpy().copy(), hC.numpy().copy()
+    e2e_pageable_s = e2e_time(nA.ctypes.data, nB.ctypes.data, nC.ctypes.data)
+    del nA, nB, nC
     lib.sgemm_cuda_finish()
-    e2e_s = max_over_ranks(e2e_s, world, torch.device("cuda", local))
 
     pk, pk_kind = peaks()
     tflops_split = flops / (ms_split * 1e-3) / 1e12
@@ -556,7 +564,7 @@ def main():
                               "worst_row_err_fp64": errs_main[p][1],
                               "wide40_4096_err_fp64": dict(zip(("normwise", "worst_row",
                                                                  "worst_col"), errs_wide[p])),
-                              "piece_products": split_forms[p]} for p in split_forms},
+                              "piece_products_16bit_rate": split_forms[p]} for p in split_forms},
             "simt_fp32": {"tflops": round(tflops_simt, 3), "normwise_err_fp64": err_simt,
                           "worst_row_err_fp64": errs_main["simt"][1],
                           "wide40_4096_err_fp64": dict(zip(("normwise", "worst_row", "worst_col"),
@@ -579,7 +587,11 @@ def main():
                                    "piece products; achieved = 2MNK / kernel time"},
         "e2e": {"value": round(whole_job_rate(flops, e2e_s, world) / 1e12, 3), "unit": "TFLOPS",
                 "h2d_bytes_per_step": 3 * M * N * 4, "d2h_bytes_per_step": M * N * 4,
-                "api": "sgemm_cuda (compat, host pointers, pinned)"},
+                "api": "sgemm_cuda (compat, host pointers, pinned)",
+                "pageable": {"value": round(whole_job_rate(flops, e2e_pageable_s, world) / 1e12, 3),
+                             "unit": "TFLOPS", "ms": round(e2e_pageable_s * 1e3, 3),
+                             "api": "sgemm_cuda on plain numpy arrays (pageable host memory)"},
+                "ms": round(e2e_s * 1e3, 3)},
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clocks,
     }

@@ -54,6 +54,9 @@ typedef enum {
   UGEMM_PREC_FP16X3 = 5, /* 2 fp16 pieces per element, every row of op(A) and column of op(B)
                             scaled by its own power of two; 3 products (tcgen05): 22-bit
                             operands, half the MMAs of BF16X6 */
+  UGEMM_PREC_TF32X3 = 6, /* 2 tf32 pieces per element (FP32's exponent range, no scaling),
+                            3 products on the tf32 tensor path (tcgen05 kind::tf32, half the
+                            16-bit rate): 22-bit operands */
 } ugemm_precision;
 
 /* ------------------------------------------------------------------ */

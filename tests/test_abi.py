@@ -139,6 +139,14 @@ def test_fp16x3_workspace_has_two_pieces_and_scale_words(lib):
         2 * (2 * 1000 * 512 * 2 + 4096)
 
 
+def test_tf32x3_workspace_has_two_four_byte_pieces(lib):
+    # two tf32 pieces (FP32 containers) per element, no scale words
+    n = ug.workspace_bytes("N", "N", 1536, 1536, 512, 512, 1536, "tf32x3")
+    assert n == 2 * (2 * 1536 * 512 * 4)
+    assert ug.workspace_bytes("T", "T", 1000, 1000, 33, 1000, 33, "tf32x3") == \
+        2 * (2 * 1000 * 64 * 4)
+
+
 def test_fast_division_constants_are_exact():
     """The implicit im2col gather divides pixel and tap indices by run-time
     constants with q = (umulhi(x, m) + x) >> s (internal.h FastDiv);

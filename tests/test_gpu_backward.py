@@ -78,7 +78,7 @@ def run_backward(ta, tb, M, N, K, alpha, prec, seed, beta_acc=0.0):
     return A, B, W, dA0, dB0, dA, dB
 
 
-@pytest.mark.parametrize("prec", ["simt", "bf16x6", "fp16x3"])
+@pytest.mark.parametrize("prec", ["simt", "bf16x6", "fp16x3", "tf32x3"])
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
 def test_backward_small_vs_fp64(prec, ta, tb):
     M, N, K = 150, 97, 203

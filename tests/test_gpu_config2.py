@@ -4,14 +4,13 @@ four transpose pairs, on U[-1,1) inputs and on wide-range sets (mantissa
 U[1,2), random sign, exponent uniform in [-8, 8], and in [-40, 40]); error
 of every form against the GPU FP64 oracle (ugemm_dgemm_oracle_dev),
 normwise, in the worst row and in the worst column (which a form that loses
-whole rows or columns to a scale cannot pass).  Both split forms (BF16x6 and
-FP16x3) must be at least as accurate as the FP32 SIMT form in all three on
-every case but one: with exponents spread over [-40, 40] and k = 1023, each
-element of C is dominated by a few products, which SIMT's fused
-multiply-add computes exactly, while the split forms drop terms of about
-2^-24 of each product (BF16x6: a1b2 + a2b1; FP16x3 keeps 22 of 24 bits);
-there both stay within 2x of SIMT's error and below 1e-6 (measured 1.4-1.6x;
-at k = 8192 on the same set both are below SIMT)."""
+whole rows or columns to a scale cannot pass).  Every split form (BF16x6,
+FP16x3, TF32x3) must be at least as accurate as the FP32 SIMT form in all
+three on every case.  The hardest is exponents spread over [-40, 40] at
+k = 1023: each element of C is dominated by a few products, which SIMT's
+fused multiply-add computes exactly, so SIMT's error is at its smallest;
+the split forms meet it with their main accumulator drained every 64 k at
+that depth."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -53,7 +52,7 @@ def errors(ta, tb, M, N, K, kind, seed):
     C0 = draw((M, N), kind, g)
     ref = ug.ref64(ta, tb, A, B, C0, ALPHA, BETA)
     out = {}
-    for prec in ("simt", "bf16x6", "fp16x3"):
+    for prec in ("simt", "bf16x6", "fp16x3", "tf32x3"):
         C = C0.clone()
         ug.sgemm_dev(ta, tb, M, N, K, ALPHA, A, A.stride(0), B, B.stride(0), BETA, C, N,
                      precision=prec)
@@ -71,11 +70,7 @@ def test_split_at_least_as_accurate_as_simt(shape, ta, tb, kind):
     e = errors(ta, tb, M, N, K, kind, seed=M + 2 * N + 3 * K + ord(ta) + 5 * ord(tb) + len(kind))
     print(f"{shape} {ta}{tb} {kind}: (normwise, worst row, worst column) " +
           " ".join(f"{p} {v[0]:.2e}/{v[1]:.2e}/{v[2]:.2e}" for p, v in e.items()))
-    few_products = kind == "wide40" and K < 4096
-    for prec in ("bf16x6", "fp16x3"):
+    for prec in ("bf16x6", "fp16x3", "tf32x3"):
         for i in range(3):
-            if few_products:
-                assert e[prec][i] <= 2 * e["simt"][i] and e[prec][i] < 1e-6, (prec, i, e)
-            else:
-                assert e[prec][i] <= e["simt"][i], (prec, i, e)
+            assert e[prec][i] <= e["simt"][i], (prec, i, e)
     assert e["simt"][0] < 1e-5

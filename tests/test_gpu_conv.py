@@ -166,7 +166,7 @@ def test_conv_stack_graph_replay_is_deterministic():
     stack.close()
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "fp16x3", "tf32x3", "simt"])
 def test_implicit_im2col_equals_explicit(prec):
     """Gathering col inside the operand pass reads exactly the values the
     im2col pass would have stored: every Y and the top layer's dW are

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 import ugemm_gb300 as ug  # noqa: E402
 
-FORMS = ("simt", "bf16x6", "bf16x9", "fp16x3")
+FORMS = ("simt", "bf16x6", "bf16x9", "fp16x3", "tf32x3")
 # Normwise relative error bound vs FP64 for the FP32-accurate forms at the
 # small sizes below (FP32 unit roundoff is 6e-8; observed errors ~1e-7).
 TOL_FP32 = 2e-6

@@ -66,7 +66,7 @@ def test_config4_grouped_256_problems(prec, graph):
     plan.close()
 
 
-@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9", "fp16x3", "simt"])
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x9", "fp16x3", "tf32x3", "simt"])
 def test_grouped_edge_cases(prec):
     """Tiny, ragged, K = 0, alpha = 0 and padded leading dimensions."""
     shapes = [("N", "N", 1, 1, 1), ("T", "T", 3, 5, 7), ("N", "T", 129, 257, 33),

@@ -2,7 +2,11 @@
 sgemm_cuda calls run as k slabs accumulated on the device, then row bands
 that finish the rest of k and go back while later bands compute; the
 result must equal an FP64 GEMM of the same operands, for every transpose
-pair, beta == 0 and beta != 0, padded leading dimensions, in both forms."""
+pair, beta == 0 and beta != 0, padded leading dimensions, in both forms.
+The operands here are plain numpy arrays -- pageable memory, as the
+reference's callers pass (sgemm_test.c's static arrays) -- which the path
+reads with copy kernels where the device addresses pageable memory; pinned
+buffers (copy engines) must give the same bits."""
 import numpy as np
 import pytest
 
@@ -62,6 +66,37 @@ def test_compat_sgemm_cuda_large_call():
     finally:
         ug.sgemm_cuda_finish()
     assert float(np.linalg.norm(C.astype(np.float64) - ref) / np.linalg.norm(ref)) < 2e-6
+
+
+@pytest.mark.parametrize("prec", ["fp16x3", "bf16x6"])
+def test_compat_8192_on_pageable_numpy_arrays(prec):
+    """sgemm_cuda at 8192^3 on plain numpy arrays (pageable), the arena sized
+    as sgemm_test.c sizes it, against the GPU FP64 oracle; the same call on
+    pinned copies of the operands gives the same bits."""
+    M = N = K = 8192
+    rng = np.random.default_rng(8192)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    C0 = rng.uniform(-1, 1, (M, N)).astype(np.float32)
+    dev = torch.device("cuda")
+    ref = ug.ref64("N", "N", torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev),
+                   torch.from_numpy(C0).to(dev), 1.5, 0.5)
+    C = C0.copy()
+    ug.sgemm_cuda_init(0, 0, (M * K + K * N + M * N) * 10 * 4)
+    try:
+        ug.set_precision(prec)
+        ug.sgemm_cuda("N", "N", M, N, K, 1.5, A, B, 0.5, C)
+        hA, hB = torch.from_numpy(A).pin_memory(), torch.from_numpy(B).pin_memory()
+        hC = torch.from_numpy(C0).pin_memory()
+        ug._check(ug.load().sgemm_cuda_status(b"N", b"N", M, N, K, 1.5, hA.data_ptr(),
+                                              hB.data_ptr(), 0.5, hC.data_ptr()))
+    finally:
+        ug.set_precision("auto")
+        ug.sgemm_cuda_finish()
+    got = torch.from_numpy(C).to(dev, torch.float64)
+    err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    assert err < 2e-6, err
+    assert np.array_equal(C, hC.numpy())
 
 
 def run_counted(prec, ta, tb, M, N, K, alpha, beta, seed):

@@ -60,6 +60,19 @@ def bf16(x):
     return ((b + r) & 0xFFFF0000).astype(np.uint32).view(np.float32)
 
 
+def tf32(x):
+    """Round to nearest (ties away from zero) to TF32's 10 stored significand
+    bits, as FP32 (the PTX cvt.rna.tf32.f32 rounding)."""
+    b = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+    return (((b + 0x1000) & 0xFFFFE000) & 0xFFFFFFFF).astype(np.uint32).view(np.float32)
+
+
+def split_tf32(x):
+    x0 = tf32(x)
+    x1 = tf32((x - x0).astype(np.float32))
+    return x0.astype(np.float64), x1.astype(np.float64)
+
+
 def split_bf16(x):
     x0 = bf16(x)
     x1 = bf16((x - x0).astype(np.float32))
@@ -87,8 +100,13 @@ def test_split_errors_against_fp64(kind):
     y0, y1, y2 = split_bf16(B)
     bf16x6 = x0 @ y0 + x0 @ y1 + x1 @ y0 + x0 @ y2 + x2 @ y0 + x1 @ y1
     assert np.array_equal(x0 + x1 + x2, A.astype(np.float64))  # three bf16 pieces are exact
+    t0, t1 = split_tf32(A)
+    u0, u1 = split_tf32(B)
+    tf32x3 = t0 @ u0 + t0 @ u1 + t1 @ u0
     e16 = np.linalg.norm(fp16x3 - exact) / norm
     ebf = np.linalg.norm(bf16x6 - exact) / norm
+    etf = np.linalg.norm(tf32x3 - exact) / norm
+    assert etf < 1.2e-7, etf      # the same 22 bits as FP16x3, no scaling
     assert e16 < 1.2e-7, e16      # ~6.5e-8: the 2^-22 dropped terms
     assert ebf < 1e-8, ebf        # ~4.5e-9: the 2^-24 dropped terms
 

@@ -41,8 +41,9 @@ PREC_BF16X6 = 2
 PREC_BF16X9 = 3
 PREC_BF16X3 = 4
 PREC_FP16X3 = 5
+PREC_TF32X3 = 6
 PRECISIONS = {"auto": PREC_AUTO, "simt": PREC_SIMT, "bf16x6": PREC_BF16X6, "bf16x9": PREC_BF16X9,
-              "bf16x3": PREC_BF16X3, "fp16x3": PREC_FP16X3}
+              "bf16x3": PREC_BF16X3, "fp16x3": PREC_FP16X3, "tf32x3": PREC_TF32X3}
 
 # Every symbol include/sgemm_cuda.h declares.
 EXPORTS = (

@@ -181,7 +181,7 @@ int resolve_form(int precision, const Gemm& g) {
 
 bool is_split_form(int form) {
   return form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9 || form == UGEMM_PREC_BF16X3 ||
-         form == UGEMM_PREC_FP16X3;
+         form == UGEMM_PREC_FP16X3 || form == UGEMM_PREC_TF32X3;
 }
 
 size_t scratch_for(const Gemm& g, int form) {
@@ -413,7 +413,7 @@ void sgemm_cuda_init(int platform, int device, size_t size) {
 }
 
 int sgemm_cuda_set_precision(int precision) {
-  if (precision < UGEMM_PREC_AUTO || precision > UGEMM_PREC_FP16X3) return UGEMM_ERR_ARG;
+  if (precision < UGEMM_PREC_AUTO || precision > UGEMM_PREC_TF32X3) return UGEMM_ERR_ARG;
   std::lock_guard<std::mutex> lock(g_mu);
   g_default_precision = precision;
   g_compat.precision = precision;

@@ -299,7 +299,7 @@ UGEMM_API int ugemm_conv_stack_create(int nlayers, const ugemm_conv_layer* layer
   s->batch = batch;
   s->form = precision == UGEMM_PREC_AUTO ? UGEMM_PREC_BF16X6 : precision;
   s->explicit_col = (flags & UGEMM_CONV_IM2COL) != 0;
-  if (s->form < UGEMM_PREC_SIMT || s->form > UGEMM_PREC_FP16X3) {
+  if (s->form < UGEMM_PREC_SIMT || s->form > UGEMM_PREC_TF32X3) {
     destroy_stack(s);
     return UGEMM_ERR_ARG;
   }

@@ -147,7 +147,7 @@ ugemm_tile_config default_grouped_config(int form) {
     c.block_n = 128;
   } else {
     c.block_n = 256;
-    c.chunk_k = split_default_chunk_kb() * kTcKB;
+    c.chunk_k = split_default_chunk_kb(1 << 30) * kTcKB;
   }
   c.max_ctas = 0;
   return c;
@@ -167,7 +167,7 @@ UGEMM_API int ugemm_grouped_plan_create(int count, const ugemm_problem* problems
   if (count <= 0 || !problems) return plan_fail(UGEMM_ERR_ARG, "empty problem list");
   int form = precision;
   if (form == UGEMM_PREC_AUTO) form = UGEMM_PREC_BF16X6;
-  if (form < UGEMM_PREC_SIMT || form > UGEMM_PREC_FP16X3)
+  if (form < UGEMM_PREC_SIMT || form > UGEMM_PREC_TF32X3)
     return plan_fail(UGEMM_ERR_ARG, "unknown precision");
   // validate and normalise
   std::vector<Gemm> g(count);
@@ -227,7 +227,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   }
   if (form != UGEMM_PREC_SIMT) {
     if (p->cfg.block_n != 128 && p->cfg.block_n != 256) p->cfg.block_n = 256;
-    if (p->cfg.chunk_k < kTcKB) p->cfg.chunk_k = split_default_chunk_kb() * kTcKB;
+    if (p->cfg.chunk_k < kTcKB) p->cfg.chunk_k = split_default_chunk_kb(1 << 30) * kTcKB;
   } else if (p->cfg.block_n != 64 && p->cfg.block_n != 128) {
     p->cfg.block_n = 128;
   }

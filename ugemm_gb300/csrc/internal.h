@@ -222,7 +222,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
                                 ugemm_grouped_plan** out);
 ugemm_tile_config default_grouped_config(int form);
 bool tuned_config(int count, const ugemm_problem* problems, int precision, ugemm_tile_config* cfg);
-int split_default_chunk_kb();
+int split_default_chunk_kb(int K);
 
 // Host-pointer GEMM with overlapped copies (k slabs, then row bands of C); returns
 // UGEMM_ERR_UNSUPPORTED when the call is too small or the arena too tight,

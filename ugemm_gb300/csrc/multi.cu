@@ -191,8 +191,9 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
   int4* recs = reinterpret_cast<int4*>(tab + align_up(sizeof(MultiTable), 256));
   MultiTable t;
   std::memset(&t, 0, sizeof t);
-  const auto* ap = static_cast<const __nv_bfloat16*>(a_pieces) + size_t(tail.r0) * Kp;
-  const auto* bp = static_cast<const __nv_bfloat16*>(b_pieces) + size_t(tail.c0) * Kp;
+  const size_t row_bytes = size_t(Kp) * piece_bytes(p.pieces);
+  const auto* ap = static_cast<const uint8_t*>(a_pieces) + size_t(tail.r0) * row_bytes;
+  const auto* bp = static_cast<const uint8_t*>(b_pieces) + size_t(tail.c0) * row_bytes;
   if (!split_encode_view(p.pieces, kTcBM, ap, Mt, g.M, g.K, &t.maps[0]) ||
       !split_encode_view(p.pieces, p.block_n, bp, Nt, g.N, g.K, &t.maps[1]))
     return UGEMM_ERR_CUDA;
@@ -230,7 +231,7 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
   const int chunk =
-      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb(g.K));
   ugemm_status s = split_gemm_launch(
       q, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
       reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), recs, tiles, chunk,
@@ -312,6 +313,8 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
       red_max = std::max(red_max, static_cast<long long>(g.M) * g.N);
     }
   }
+  int min_k = gs[0].K;  // the chunk rule follows the shallowest GEMM (the most accurate choice)
+  for (int i = 1; i < n; ++i) min_k = std::min(min_k, gs[i].K);
   // longest k first; tile offsets in that order
   std::stable_sort(t.probs, t.probs + nsub,
                    [](const TcProblem& a, const TcProblem& b) { return a.nkb > b.nkb; });
@@ -328,7 +331,7 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
   const int chunk =
-      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb(min_k));
   ugemm_status s = split_gemm_launch(
       p, dummy, dummy, single, reinterpret_cast<const CUtensorMap*>(tab + offsetof(MultiTable, maps)),
       reinterpret_cast<const TcProblem*>(tab + offsetof(MultiTable, probs)), recs, tiles, chunk,

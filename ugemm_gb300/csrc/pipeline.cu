@@ -26,9 +26,27 @@
 // 16-byte pitches so that TMA can describe them whatever the host leading
 // dimensions are; in the split forms each slab and band is split into bf16
 // pieces once, on its own stream, while the previous GEMM runs.
+//
+// Host buffers.  The reference's callers pass pageable memory (sgemm_test.c
+// declares `static float A[...]` and hands it to sgemm_ocl, whose oclWrite
+// copies it, sgemm_ocl2.h:173-176).  A cudaMemcpyAsync from pageable memory
+// returns only when the copy is done, which would serialise every copy and
+// launch behind it.  Where the device can address pageable memory itself
+// (a Grace host: NVLink-C2C with address translation; measured 201 GB/s of
+// kernel reads against 210 GB/s pinned copies), the reads of pageable
+// buffers -- A, B and the incoming C, whose pages hold the caller's data --
+// are stream-ordered copy kernels on the copy streams (a few dozen CTAs,
+// which fit beside a running GEMM's); the bands of C go back with the copy
+// engines, enqueued after every GEMM of the call, so that a copy that
+// returns only when done costs no overlap.  Where the device cannot address
+// pageable memory, the call registers the buffers' ranges for its duration
+// (cudaHostRegister) so that the copy engines run every copy asynchronously.
+// Pinned buffers use the copy engines.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -86,10 +104,135 @@ ugemm_status pipe_state(PipeState** out) {
 
 bool is_split(int form) {
   return form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9 || form == UGEMM_PREC_BF16X3 ||
-         form == UGEMM_PREC_FP16X3;
+         form == UGEMM_PREC_FP16X3 || form == UGEMM_PREC_TF32X3;
 }
 
 int pitch4(int n) { return static_cast<int>(align_up(n, 4)); }
+
+// A 2-D copy of `rows` rows of `width` bytes (a multiple of 4) between
+// pitched buffers, either of which may be pageable host memory the device
+// addresses directly.  Blocks take rows grid-stride; each thread keeps four
+// 16-byte (or 4-byte) loads in flight before storing them, which covers the
+// host link's latency with a few dozen CTAs.
+template <typename T>
+__global__ void __launch_bounds__(256) copy2d_kernel(const uint8_t* __restrict__ src, size_t spitch,
+                                                     uint8_t* __restrict__ dst, size_t dpitch,
+                                                     size_t width, int rows) {
+  const size_t n = width / sizeof(T);
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const T* s = reinterpret_cast<const T*>(src + size_t(r) * spitch);
+    T* d = reinterpret_cast<T*>(dst + size_t(r) * dpitch);
+    for (size_t c = threadIdx.x; c < n; c += 4 * 256) {
+      T v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const size_t i = c + size_t(u) * 256;
+        if (i < n) v[u] = s[i];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const size_t i = c + size_t(u) * 256;
+        if (i < n) d[i] = v[u];
+      }
+    }
+  }
+}
+
+// CTAs of one copy kernel (UGEMM_COPY_CTAS overrides): enough bytes in
+// flight for the host link.
+int copy_ctas() {
+  static const int n = [] {
+    const char* e = std::getenv("UGEMM_COPY_CTAS");
+    const int v = e ? std::atoi(e) : 0;
+    return v > 0 ? v : 48;
+  }();
+  return n;
+}
+
+bool copy2d_launch(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, int rows,
+                   cudaStream_t st) {
+  if (rows <= 0 || width == 0) return true;
+  const auto* s = static_cast<const uint8_t*>(src);
+  auto* d = static_cast<uint8_t*>(dst);
+  const int grid = std::min(rows, copy_ctas());
+  const bool vec = ((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d) | spitch |
+                     dpitch | width) & 15) == 0;
+  if (vec) copy2d_kernel<float4><<<grid, 256, 0, st>>>(s, spitch, d, dpitch, width, rows);
+  else copy2d_kernel<float><<<grid, 256, 0, st>>>(s, spitch, d, dpitch, width, rows);
+  return cudaPeekAtLastError() == cudaSuccess;
+}
+
+// Whether the current device can read and write pageable host memory
+// directly (address translation through the host's page tables).
+bool device_reads_pageable() {
+  static int cached[64];
+  static std::once_flag once[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  std::call_once(once[dev], [dev] {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev);
+    cached[dev] = v;
+  });
+  return cached[dev] != 0;
+}
+
+// How the copies of one host buffer cross the link: the copy engines (pinned
+// or registered memory), copy kernels (reads of pageable memory the device
+// addresses), or the copy engines after registering the buffer for the call.
+enum class Xfer { kEngine, kKernel, kRegistered };
+
+bool is_pageable(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return true;
+  }
+  return a.type == cudaMemoryTypeUnregistered;
+}
+
+// The buffers a call registered, released when it returns (after the
+// device is idle: an early error return may leave copies in flight).
+struct Registrations {
+  std::vector<void*> ptrs;
+  ~Registrations() {
+    if (ptrs.empty()) return;
+    cudaDeviceSynchronize();
+    for (void* p : ptrs) cudaHostUnregister(p);
+  }
+};
+
+// UGEMM_PAGEABLE selects how pageable buffers travel where the device
+// addresses them: "kernel" (the default: reads by copy kernels, C back by the
+// copy engines), "kernel_all" (C back by a copy kernel too) or "register"
+// (every buffer registered for the call, all copies by the copy engines).
+int pageable_mode() {
+  static const int m = [] {
+    const char* e = std::getenv("UGEMM_PAGEABLE");
+    if (e && std::strcmp(e, "kernel_all") == 0) return 1;
+    if (e && std::strcmp(e, "register") == 0) return 2;
+    return 0;
+  }();
+  return m;
+}
+
+Xfer xfer_for(const void* p, size_t bytes, Registrations& regs) {
+  if (!p || bytes == 0 || !is_pageable(p)) return Xfer::kEngine;
+  if (device_reads_pageable() && pageable_mode() != 2) return Xfer::kKernel;
+  void* q = const_cast<void*>(p);
+  if (cudaHostRegister(q, bytes, cudaHostRegisterDefault) == cudaSuccess) {
+    regs.ptrs.push_back(q);
+    return Xfer::kRegistered;
+  }
+  (void)cudaGetLastError();
+  return Xfer::kEngine;  // pageable copies that return when done: correct, not overlapped
+}
+
+bool copy2d(Xfer x, void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
+            int rows, cudaMemcpyKind kind, cudaStream_t st) {
+  if (x == Xfer::kKernel) return copy2d_launch(dst, dpitch, src, spitch, width, rows, st);
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, st) == cudaSuccess;
+}
 
 // Layout of one pipelined call: k1 = depth of the slab phase (0: bands
 // only), the slab width and band height, the device pitches and the bytes of
@@ -228,6 +371,18 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   std::lock_guard<std::mutex> lock(g_pmu);
   PipeState* ps = nullptr;
   if (pipe_state(&ps) != UGEMM_OK) return UGEMM_ERR_CUDA;
+  // how each host buffer crosses the link (registrations end with the call,
+  // after its last copy has been waited for)
+  Registrations regs;
+  const size_t a_span = ((g.ta == 'N' ? size_t(g.M) : size_t(g.K)) - 1) * g.lda +
+                        (g.ta == 'N' ? g.K : g.M);
+  const size_t b_span = ((g.tb == 'N' ? size_t(g.K) : size_t(g.N)) - 1) * g.ldb +
+                        (g.tb == 'N' ? g.N : g.K);
+  const size_t c_span = (size_t(g.M) - 1) * g.ldc + g.N;
+  const Xfer xa = xfer_for(g.A, a_span * 4, regs), xb = xfer_for(g.B, b_span * 4, regs);
+  const Xfer xc = xfer_for(g.C, c_span * 4, regs);
+  const Xfer xc_out =  // C goes back by the copy engines unless asked otherwise
+      xc == Xfer::kKernel && pageable_mode() != 1 ? Xfer::kEngine : xc;
   uint8_t* base = static_cast<uint8_t*>(arena);
   size_t off = 0;
   auto take = [&](size_t n) { uint8_t* p = base + off; off += n; return p; };
@@ -252,16 +407,16 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   auto copy_a = [&](int m0, int mr, int k0, int kw) {
     const int r0 = g.ta == 'N' ? m0 : k0, c0 = g.ta == 'N' ? k0 : m0;
     const int nr = g.ta == 'N' ? mr : kw, nc = g.ta == 'N' ? kw : mr;
-    return ck(cudaMemcpy2DAsync(dA + size_t(r0) * lda_d + c0, size_t(lda_d) * 4,
-                                g.A + size_t(r0) * g.lda + c0, size_t(g.lda) * 4, size_t(nc) * 4,
-                                nr, cudaMemcpyHostToDevice, ps->h2d));
+    return copy2d(xa, dA + size_t(r0) * lda_d + c0, size_t(lda_d) * 4,
+                  g.A + size_t(r0) * g.lda + c0, size_t(g.lda) * 4, size_t(nc) * 4, nr,
+                  cudaMemcpyHostToDevice, ps->h2d);
   };
   auto copy_b = [&](int k0, int kw) {  // all N columns of op(B), k rows k0..k0+kw
     const int r0 = g.tb == 'N' ? k0 : 0, c0 = g.tb == 'N' ? 0 : k0;
     const int nr = g.tb == 'N' ? kw : g.N, nc = g.tb == 'N' ? g.N : kw;
-    return ck(cudaMemcpy2DAsync(dB + size_t(r0) * ldb_d + c0, size_t(ldb_d) * 4,
-                                g.B + size_t(r0) * g.ldb + c0, size_t(g.ldb) * 4, size_t(nc) * 4,
-                                nr, cudaMemcpyHostToDevice, ps->h2d));
+    return copy2d(xb, dB + size_t(r0) * ldb_d + c0, size_t(ldb_d) * 4,
+                  g.B + size_t(r0) * g.ldb + c0, size_t(g.ldb) * 4, size_t(nc) * 4, nr,
+                  cudaMemcpyHostToDevice, ps->h2d);
   };
   auto a_view = [&](int m0, int k0) { return dA + m0 * a_sr + k0 * a_sk; };
   auto b_view = [&](int k0) { return dB + k0 * b_sk; };
@@ -282,9 +437,8 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
     const int m0 = L.band_m0[r], mb = L.band_h[r];
     if (!copy_a(m0, mb, k1, k2)) return UGEMM_ERR_CUDA;
     if (g.beta != 0.f &&  // beta == 0: C is not read (sgemm_ocl2.h:177)
-        !ck(cudaMemcpy2DAsync(dCin + size_t(m0) * ldc_d, size_t(ldc_d) * 4,
-                              g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, size_t(g.N) * 4, mb,
-                              cudaMemcpyHostToDevice, ps->h2d)))
+        !copy2d(xc, dCin + size_t(m0) * ldc_d, size_t(ldc_d) * 4, g.C + size_t(m0) * g.ldc,
+                size_t(g.ldc) * 4, size_t(g.N) * 4, mb, cudaMemcpyHostToDevice, ps->h2d))
       return UGEMM_ERR_CUDA;
     if (!ck(cudaEventRecord(ps->band_in[r], ps->h2d))) return UGEMM_ERR_CUDA;
   }
@@ -359,10 +513,15 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
                             : simt_launch(gb, simt_pick_tile(gb), Scratch{nullptr, 0}, dev_err,
                                           gs_st);
     if (st != UGEMM_OK || !ck(cudaEventRecord(ps->band_done[r], gs_st))) return UGEMM_ERR_CUDA;
+  }
+  // ---- finished bands back to the host, each as soon as its GEMM is done
+  // (enqueued after all the GEMMs: a copy into pageable memory returns only
+  // when done)
+  for (int r = 0; r < L.nband; ++r) {
+    const int m0 = L.band_m0[r], mb = L.band_h[r];
     cudaStreamWaitEvent(ps->d2h, ps->band_done[r], 0);
-    if (!ck(cudaMemcpy2DAsync(g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, dC + size_t(m0) * ldc_d,
-                              size_t(ldc_d) * 4, size_t(g.N) * 4, mb, cudaMemcpyDeviceToHost,
-                              ps->d2h)))
+    if (!copy2d(xc_out, g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, dC + size_t(m0) * ldc_d,
+                size_t(ldc_d) * 4, size_t(g.N) * 4, mb, cudaMemcpyDeviceToHost, ps->d2h))
       return UGEMM_ERR_CUDA;
   }
   // the caller's stream resumes after the last copy back

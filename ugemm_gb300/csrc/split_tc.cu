@@ -115,13 +115,20 @@ __device__ __forceinline__ TileCoord tile_coord(const TcProblem& single, const T
   return tc;
 }
 
-template <int NP, int BN, bool GROUPED, bool EPI>
+// TF32: the TF32x3 form's instantiation (two planes of 32-deep tf32
+// stages, tcgen05 kind::tf32), a template parameter so that the 16-bit
+// instantiations' MMA issue loop carries no branch on the format.
+template <int NP, int BN, bool GROUPED, bool EPI, bool TF32 = false>
 __global__ void __launch_bounds__(kTcThreads, 1)
     split_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
                     const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                     int total_tiles, int nprod,
-                    int chunk_kb, int f16, int* err) {
+                    int chunk_kb, int fmt, int* err) {
+  // fmt: 16-bit piece format, 0 bf16, 1 fp16 (FP16x3); TF32 instantiations
+  // read two planes of 32-deep stages with the 128-byte rows of the
+  // two-piece 16-bit shape
+  static_assert(!TF32 || NP == 2, "TF32 pieces come in two planes");
   constexpr bool WIDE = split_stage_k(NP) > kTcKB;
   using S = TcShape<NP, BN, WIDE>;
   constexpr int KB = S::KB;
@@ -183,14 +190,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           fence_tensormap(mb);
         }
         const int kb0 = GROUPED ? P.kb0 : 0;  // first k-block of a split-K slice
+        constexpr int kx = TF32 ? KB / 2 : KB;  // elements of k per stage
         for (int kb = 0; kb < P.nkb; ++kb, ++it) {
           const int s = it % S::STAGES;
           const uint32_t ph = (it / S::STAGES) & 1;
           if (!mbar_wait(&empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
           uint8_t* sa = smem + s * S::STAGE_BYTES;
           mbar_arrive_expect_tx(&full[s], S::STAGE_BYTES);
-          tma_load_3d(sa, ma, &full[s], (kb0 + kb) * KB, tc.m0, 0);
-          tma_load_3d(sa + S::A_BYTES, mb, &full[s], (kb0 + kb) * KB, tc.n0, 0);
+          tma_load_3d(sa, ma, &full[s], (kb0 + kb) * kx, tc.m0, 0);
+          tma_load_3d(sa + S::A_BYTES, mb, &full[s], (kb0 + kb) * kx, tc.n0, 0);
         }
       }
       if (!ok) {  // let copies still in flight land before the CTA exits
@@ -201,9 +209,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      // operand format: bf16 pieces (1) or the FP16x3 form's fp16 pieces (0)
-      const uint32_t fmt = (NP == 2 && f16) ? 0u : 1u;
-      const uint32_t idesc_full = umma_idesc(fmt, fmt, kTcBM, BN);
+      // instruction descriptor operand format: bf16 pieces (1), the FP16x3
+      // form's fp16 pieces (0) or the TF32x3 form's tf32 pieces (2); one
+      // k step is 32 bytes of a row in each: 16 16-bit or 8 tf32 elements
+      const uint32_t ifmt = TF32 ? 2u : (NP == 2 && fmt == 1 ? 0u : 1u);
+      const uint32_t idesc_full = umma_idesc(ifmt, ifmt, kTcBM, BN);
       const uint32_t base = smem_u32(smem);
       uint32_t it = 0, ntile = 0;
       uint32_t nbound[NB] = {};
@@ -217,7 +227,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         uint32_t idesc = idesc_full;
         if constexpr (GROUPED) {
           const int n_rem = P.N - tc.n0;
-          if (n_rem < BN) idesc = umma_idesc(fmt, fmt, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
+          if (n_rem < BN) idesc = umma_idesc(ifmt, ifmt, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
         }
         const uint32_t buf = ntile % NB, use = ntile / NB;
         const uint32_t t_main = tmem + buf * 2 * BN, t_corr = t_main + BN;
@@ -239,10 +249,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t code = kCorrections[p];
             const uint32_t ia = code >> 2, ib = code & 3;
 #pragma unroll
-            for (int kk = 0; kk < KB / 16; ++kk)
-              umma_bf16(t_corr, umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, SBO, SWZ),
-                        umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, SBO, SWZ), idesc,
-                        (kb | p | kk) != 0);
+            for (int kk = 0; kk < KB / 16; ++kk) {
+              const uint64_t da = umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, SBO, SWZ);
+              const uint64_t db = umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, SBO, SWZ);
+              if constexpr (TF32) umma_tf32(t_corr, da, db, idesc, (kb | p | kk) != 0);
+              else umma_bf16(t_corr, da, db, idesc, (kb | p | kk) != 0);
+            }
           }
           // main product; a new chunk restarts the accumulator once drained
           const bool chunk_start = (kb % chunk_kb) == 0;
@@ -255,9 +267,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             tc_fence_after();
           }
 #pragma unroll
-          for (int kk = 0; kk < KB / 16; ++kk)
-            umma_bf16(t_main, umma_smem_desc(sa + kk * 32, SBO, SWZ),
-                      umma_smem_desc(sb + kk * 32, SBO, SWZ), idesc, !(chunk_start && kk == 0));
+          for (int kk = 0; kk < KB / 16; ++kk) {
+            const uint64_t da = umma_smem_desc(sa + kk * 32, SBO, SWZ);
+            const uint64_t db = umma_smem_desc(sb + kk * 32, SBO, SWZ);
+            if constexpr (TF32) umma_tf32(t_main, da, db, idesc, !(chunk_start && kk == 0));
+            else umma_bf16(t_main, da, db, idesc, !(chunk_start && kk == 0));
+          }
           umma_commit(&empty[s]);
           if ((kb + 1) % chunk_kb == 0 && kb + 1 < P.nkb) umma_commit(&main_full[buf]);
         }
@@ -486,12 +501,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 // ---------------------------------------------------------------- split pass
 // Pieces of two consecutive k of one row, each piece plane as one packed
-// 16-bit pair: bf16 pieces (x0 = bf16(x), x1 = bf16(x - x0), ...) or, with
-// F16, the FP16x3 form's two fp16 pieces of x * 2^e (e = the row's
+// 16-bit pair: bf16 pieces (FMT 0: x0 = bf16(x), x1 = bf16(x - x0), ...) or
+// the FP16x3 form's two fp16 pieces of x * 2^e (FMT 1; e = the row's
 // f16_scale_exp; only two-piece operands use it).
-template <int NP, bool F16>
+template <int NP, int FMT>
 __device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t (&out)[NP]) {
-  if constexpr (F16) {
+  if constexpr (FMT == 1) {
     const float y0 = scale_pow2(x0, e), y1 = scale_pow2(x1, e);
     const __half h00 = __float2half_rn(y0), h01 = __float2half_rn(y1);
     const __half2 hi = __halves2half2(h00, h01);
@@ -527,12 +542,57 @@ __device__ __forceinline__ int f16_row_exp(const unsigned* fmax, int r) {
   return fmax ? f16_scale_exp(fmax[r]) : 0;
 }
 
+// x rounded to TF32 (10 stored significand bits, round to nearest, ties
+// away from zero), as an FP32 bit pattern with the low 13 bits clear.
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// The pieces of 8 consecutive k of one row (v[0..7]) into the planes at
+// dst + p * plane + off: one 16-byte store per plane of 16-bit pieces, two
+// per plane of TF32 pieces (FMT 2: x0 = tf32(x), x1 = tf32(x - x0); x - x0
+// is exact in FP32, and x0 + x1 keeps 22 significant bits of x).
+template <int NP, int FMT>
+__device__ __forceinline__ void store_pieces8(__nv_bfloat16* __restrict__ dst, size_t plane,
+                                              size_t off, const float (&v)[8], int ex) {
+  if constexpr (FMT == 2) {
+    uint32_t hi[8], lo[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      hi[e] = to_tf32(v[e]);
+      lo[e] = to_tf32(v[e] - __uint_as_float(hi[e]));
+    }
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    uint4* p0 = reinterpret_cast<uint4*>(d + off);
+    uint4* p1 = reinterpret_cast<uint4*>(d + plane + off);
+    p0[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    p0[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
+    p1[0] = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    p1[1] = make_uint4(lo[4], lo[5], lo[6], lo[7]);
+  } else {
+    uint32_t packed[NP][4];
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      uint32_t two[NP];
+      pieces_pair<NP, FMT>(v[e], v[e + 1], ex, two);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+      *reinterpret_cast<uint4*>(dst + p * plane + off) =
+          make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+  }
+}
+
 // One 32-row x 64-k tile of op(X) (element (r, k) at src[r*sr + k*sk]) into
 // NP bf16 planes dst[p][rows][Kp], through shared memory so that both source
 // layouts are read coalesced: float4 loads along the contiguous dimension
 // when the operand allows it, one 16-byte store of 8 k per plane per thread.
 // Zero for k >= K.
-template <int NP, bool F16>
+template <int NP, int FMT>
 __device__ __forceinline__ void split_tile(const float* __restrict__ src, long long sr,
                                            long long sk, int rows, int K, int Kp,
                                            __nv_bfloat16* __restrict__ dst, int r0, int k0,
@@ -579,31 +639,22 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ src, long l
   const int r = r0 + rr, k = k0 + g8;
   if (r < rows && k < Kp) {
     const size_t plane = static_cast<size_t>(rows) * Kp;
-    const int ex = F16 ? f16_row_exp(fmax, r) : 0;
-    uint32_t packed[NP][4];
+    const int ex = FMT == 1 ? f16_row_exp(fmax, r) : 0;
+    float v[8];
 #pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      uint32_t two[NP];
-      pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], ex, two);
-#pragma unroll
-      for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
-    }
-    const size_t off = static_cast<size_t>(r) * Kp + k;
-#pragma unroll
-    for (int p = 0; p < NP; ++p)
-      *reinterpret_cast<uint4*>(dst + p * plane + off) =
-          make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+    for (int e = 0; e < 8; ++e) v[e] = tile[rr][g8 + e];
+    store_pieces8<NP, FMT>(dst, plane, static_cast<size_t>(r) * Kp + k, v, ex);
   }
 }
 
-template <int NP, bool F16>
+template <int NP, int FMT>
 __global__ void __launch_bounds__(256) split_pieces_kernel(const float* __restrict__ src,
                                                            long long sr, long long sk, int rows,
                                                            int K, int Kp,
                                                            __nv_bfloat16* __restrict__ dst,
                                                            const unsigned* fmax) {
   __shared__ float tile[32][65];
-  split_tile<NP, F16>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile, fmax);
+  split_tile<NP, FMT>(src, sr, sk, rows, K, Kp, dst, blockIdx.y * 32, blockIdx.x * 64, tile, fmax);
 }
 
 // Raw values of one 32 x 64 tile, read with the same float4 pattern as
@@ -706,27 +757,18 @@ __device__ __forceinline__ void raw_to_smem(const SplitJob& j, const RawTile& in
 
 // bf16 pieces of one tile from shared memory: 8 consecutive k of one row per
 // thread, one 16-byte store per plane.
-template <int NP, bool F16>
+template <int NP, int FMT>
 __device__ __forceinline__ void split_store(const SplitJob& j, int r0, int k0, float (*tile)[65]) {
   const int t = threadIdx.x;
   const int rr = t >> 3, g8 = (t & 7) * 8;
   const int r = r0 + rr, k = k0 + g8;
   if (r >= j.rows || k >= j.Kp) return;
   const size_t plane = static_cast<size_t>(j.rows) * j.Kp;
-  const int ex = F16 ? f16_row_exp(j.fmax, r) : 0;
-  uint32_t packed[NP][4];
+  const int ex = FMT == 1 ? f16_row_exp(j.fmax, r) : 0;
+  float v[8];
 #pragma unroll
-  for (int e = 0; e < 8; e += 2) {
-    uint32_t two[NP];
-    pieces_pair<NP, F16>(tile[rr][g8 + e], tile[rr][g8 + e + 1], ex, two);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
-  }
-  const size_t off = static_cast<size_t>(r) * j.Kp + k;
-#pragma unroll
-  for (int p = 0; p < NP; ++p)
-    *reinterpret_cast<uint4*>(j.dst + p * plane + off) =
-        make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+  for (int e = 0; e < 8; ++e) v[e] = tile[rr][g8 + e];
+  store_pieces8<NP, FMT>(j.dst, plane, static_cast<size_t>(r) * j.Kp + k, v, ex);
 }
 
 // Many operands in one launch.  Blocks walk the tiles grid-stride; the next
@@ -752,7 +794,7 @@ __device__ __forceinline__ void tile_origin(const SplitJob& j, int b, int& r0, i
   k0 = (local % tiles_k) * 64;
 }
 
-template <int NP, bool F16>
+template <int NP, int FMT>
 __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
                                                                    int njobs, int total_tiles) {
   __shared__ float tile[32][65];
@@ -778,7 +820,7 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
       load_raw(nxt, nr0, nk0, raw);
     }
     __syncthreads();
-    split_store<NP, F16>(cur, r0, k0, tile);
+    split_store<NP, FMT>(cur, r0, k0, tile);
     __syncthreads();
     cur = nxt;
     r0 = nr0;
@@ -828,8 +870,18 @@ __global__ void __launch_bounds__(256) operand_row_max_kernel(const float* __res
     float m = 0.f;
     if (r < rows) {
       const float* row = src + r * sr;
-      if (VEC) {  // k0 and kper are multiples of 4 here
-        for (int k = k0 + 4 * l; k < k1; k += 64) {
+      if (VEC) {  // k0 and kper are multiples of 4 here; four loads in flight
+        int k = k0 + 4 * l;
+        for (; k + 192 + 3 < k1; k += 256) {
+          float4 v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = *reinterpret_cast<const float4*>(row + k + 64 * u);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            m = fmaxf(m, fmaxf(fmaxf(finite_abs(v[u].x), finite_abs(v[u].y)),
+                               fmaxf(finite_abs(v[u].z), finite_abs(v[u].w))));
+        }
+        for (; k < k1; k += 64) {
           if (k + 3 < k1) {
             const float4 v = *reinterpret_cast<const float4*>(row + k);
             m = fmaxf(m, fmaxf(fmaxf(finite_abs(v.x), finite_abs(v.y)),
@@ -849,7 +901,23 @@ __global__ void __launch_bounds__(256) operand_row_max_kernel(const float* __res
     __shared__ float part[4][256];
     const int q = t & 63, ty = t >> 6, r0 = blockIdx.x * 256 + 4 * q;
     float m[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k = k0 + ty; k < k1; k += 4) {
+    int k = k0 + ty;
+    if (VEC && r0 + 3 < rows) {  // four loads in flight
+      for (; k + 12 < k1; k += 16) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          v[u] = *reinterpret_cast<const float4*>(src + (k + 4 * u) * sk + r0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          m[0] = fmaxf(m[0], finite_abs(v[u].x));
+          m[1] = fmaxf(m[1], finite_abs(v[u].y));
+          m[2] = fmaxf(m[2], finite_abs(v[u].z));
+          m[3] = fmaxf(m[3], finite_abs(v[u].w));
+        }
+      }
+    }
+    for (; k < k1; k += 4) {
       const float* p = src + k * sk + r0;
       if (VEC && r0 + 3 < rows) {
         const float4 v = *reinterpret_cast<const float4*>(p);
@@ -899,19 +967,12 @@ __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob
   }
 }
 
-template <int NP>
+template <int NP, int FMT>
 void launch_split(const float* src, long long sr, long long sk, int rows, int K, int Kp,
                   __nv_bfloat16* dst, cudaStream_t st, const unsigned* fmax = nullptr) {
   dim3 grid(cdiv(Kp, 64), cdiv(rows, 32));
   prof_begin(st);
-  if constexpr (NP == 2) {  // the FP16x3 form has two pieces
-    if (fmax) {
-      split_pieces_kernel<2, true><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, Kp, dst, fmax);
-      prof_end(st, kProfSplitPrep);
-      return;
-    }
-  }
-  split_pieces_kernel<NP, false><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, Kp, dst, nullptr);
+  split_pieces_kernel<NP, FMT><<<grid, 256, 0, st>>>(src, sr, sk, rows, K, Kp, dst, fmax);
   prof_end(st, kProfSplitPrep);
 }
 
@@ -926,19 +987,19 @@ int sm_count() {
   return sms;
 }
 
-template <int NP, int BN, bool GROUPED, bool EPI>
+template <int NP, int BN, bool GROUPED, bool EPI, bool TF32>
 ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcProblem& single,
                            const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
-                           int total_tiles, int nprod, int chunk_kb, int max_ctas, bool f16,
+                           int total_tiles, int nprod, int chunk_kb, int max_ctas, int fmt,
                            int* dev_err, cudaStream_t st) {
   using S = TcShape<NP, BN, (split_stage_k(NP) > kTcKB)>;
-  auto kern = split_tc_kernel<NP, BN, GROUPED, EPI>;
+  auto kern = split_tc_kernel<NP, BN, GROUPED, EPI, TF32>;
   static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
   if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
   const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
   kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, tiles, total_tiles, nprod,
-                                          chunk_kb, f16 ? 1 : 0, dev_err);
+                                          chunk_kb, fmt, dev_err);
   prof_end(st, GROUPED ? kProfGrouped : kProfSplitGemm);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
@@ -992,14 +1053,21 @@ std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_
   return table;
 }
 
-int split_default_chunk_kb() {
-  static int chunk = 0;
-  if (!chunk) {
+// Depth of the main accumulator's chunks, in 32-deep k-blocks, for a GEMM
+// of depth K (UGEMM_CHUNK_K overrides).  Each chunk is summed in TMEM, whose
+// adds truncate, then drained into FP32 registers with round-to-nearest
+// adds: shorter chunks are more accurate and cost drains.  Measured on
+// GB300: 128 costs nothing against 256 at 8192^3 and takes the error at
+// 4096^3 from 3.6e-7 to 2.3e-7; at k <= 1024, where FP32 SIMT's own error is
+// smallest (a few products dominate each element when the values span many
+// binades), 64 keeps both split forms at or below it for about 5% of time.
+int split_default_chunk_kb(int K) {
+  static const int forced = [] {
     const char* e = std::getenv("UGEMM_CHUNK_K");
-    const int k = e ? std::atoi(e) : 256;
-    chunk = std::max(1, k / kTcKB);
-  }
-  return chunk;
+    return e ? std::max(1, std::atoi(e) / kTcKB) : 0;
+  }();
+  if (forced) return forced;
+  return K <= 1024 ? 2 : 4;
 }
 
 SplitPlan split_plan_for(int precision, const Gemm& g) {
@@ -1008,6 +1076,7 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
     case UGEMM_PREC_BF16X9: p.pieces = 3; p.products = 9; break;
     case UGEMM_PREC_BF16X3: p.pieces = 2; p.products = 3; break;
     case UGEMM_PREC_FP16X3: p.pieces = 2; p.products = 3; p.f16 = true; break;
+    case UGEMM_PREC_TF32X3: p.pieces = kPiecesTf32; p.products = 3; break;
     default: p.pieces = 3; p.products = 6; break;
   }
   p.block_n = (g.N > 128) ? 256 : 128;
@@ -1016,7 +1085,7 @@ SplitPlan split_plan_for(int precision, const Gemm& g) {
 }
 
 size_t split_operand_bytes(int pieces, int rows, int K) {
-  return align_up(size_t(pieces) * rows * kp_of(K) * 2, 256) +
+  return align_up(size_t(piece_planes(pieces)) * rows * kp_of(K) * piece_bytes(pieces), 256) +
          (pieces == 2 ? align_up(size_t(std::max(rows, 1)) * sizeof(unsigned), 256) : 0);
 }
 
@@ -1033,28 +1102,31 @@ size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p) {
 // Boxes of one stage: split_stage_k(pieces) deep, 128-byte swizzle for
 // 64-deep stages, 64-byte swizzle for 32-deep ones.
 CUtensorMapSwizzle split_swizzle(int pieces) {
-  return split_stage_k(pieces) > kTcKB ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  return split_stage_k(pieces) * piece_bytes(pieces) == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                                            : CU_TENSOR_MAP_SWIZZLE_64B;
+}
+
+CUtensorMapDataType piece_dtype(int pieces) {
+  return pieces == kPiecesTf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
 }
 
 bool split_encode_view(int pieces, int box_rows, const void* base, int rows, int plane_rows, int K,
                        CUtensorMap* map) {
-  const int Kp = kp_of(K);
-  const uint64_t row = uint64_t(Kp) * 2;
-  return encode_tmap_3d(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, Kp, rows, pieces, row,
-                        row * plane_rows, split_stage_k(pieces), box_rows, pieces,
-                        split_swizzle(pieces));
+  const int Kp = kp_of(K), eb = piece_bytes(pieces), np = piece_planes(pieces);
+  const uint64_t row = uint64_t(Kp) * eb;
+  return encode_tmap_3d(map, piece_dtype(pieces), eb, base, Kp, rows, np, row, row * plane_rows,
+                        split_stage_k(pieces), box_rows, np, split_swizzle(pieces));
 }
 
 bool split_encode_maps(int pieces, int block_n, const void* ap, int M, const void* bp, int N,
                        int K, CUtensorMap* ta, CUtensorMap* tb) {
-  const int Kp = kp_of(K);
-  const uint64_t row = uint64_t(Kp) * 2;
+  const int Kp = kp_of(K), eb = piece_bytes(pieces), np = piece_planes(pieces);
+  const uint64_t row = uint64_t(Kp) * eb;
   const uint32_t kb = split_stage_k(pieces);
   const CUtensorMapSwizzle sw = split_swizzle(pieces);
-  return encode_tmap_3d(ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ap, Kp, M, pieces, row, row * M,
-                        kb, kTcBM, pieces, sw) &&
-         encode_tmap_3d(tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bp, Kp, N, pieces, row, row * N,
-                        kb, block_n, pieces, sw);
+  const CUtensorMapDataType dt = piece_dtype(pieces);
+  return encode_tmap_3d(ta, dt, eb, ap, Kp, M, np, row, row * M, kb, kTcBM, np, sw) &&
+         encode_tmap_3d(tb, dt, eb, bp, Kp, N, np, row, row * N, kb, block_n, np, sw);
 }
 
 TcProblem split_problem(const Gemm& g, int pieces, int block_n, int tile_start) {
@@ -1104,19 +1176,23 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                int chunk_kb,
                                int max_ctas, int* dev_err, cudaStream_t st) {
   const bool grouped = probs != nullptr;
-#define UGEMM_SPLIT_CASE(NP, BN, GR, EPI)                                                    \
-  if (p.pieces == NP && p.block_n == BN && grouped == GR && p.epi == EPI)                   \
-    return launch_kernel<NP, BN, GR, EPI>(ta, tb, single, maps, probs, tiles, total_tiles,   \
-                                          p.products, chunk_kb, max_ctas, p.f16, dev_err, st);
-#define UGEMM_SPLIT_CASES(NP, BN)    \
-  UGEMM_SPLIT_CASE(NP, BN, false, false) \
-  UGEMM_SPLIT_CASE(NP, BN, false, true)  \
-  UGEMM_SPLIT_CASE(NP, BN, true, false)  \
-  UGEMM_SPLIT_CASE(NP, BN, true, true)
-  UGEMM_SPLIT_CASES(3, 256)
-  UGEMM_SPLIT_CASES(3, 128)
-  UGEMM_SPLIT_CASES(2, 256)
-  UGEMM_SPLIT_CASES(2, 128)
+  const int fmt = p.f16 ? 1 : 0;
+  const bool tf32 = p.pieces == kPiecesTf32;
+#define UGEMM_SPLIT_CASE(NP, BN, GR, EPI, T)                                                     \
+  if (kernel_np(p.pieces) == NP && p.block_n == BN && grouped == GR && p.epi == EPI && tf32 == T) \
+    return launch_kernel<NP, BN, GR, EPI, T>(ta, tb, single, maps, probs, tiles, total_tiles,     \
+                                             p.products, chunk_kb, max_ctas, fmt, dev_err, st);
+#define UGEMM_SPLIT_CASES(NP, BN, T)    \
+  UGEMM_SPLIT_CASE(NP, BN, false, false, T) \
+  UGEMM_SPLIT_CASE(NP, BN, false, true, T)  \
+  UGEMM_SPLIT_CASE(NP, BN, true, false, T)  \
+  UGEMM_SPLIT_CASE(NP, BN, true, true, T)
+  UGEMM_SPLIT_CASES(3, 256, false)
+  UGEMM_SPLIT_CASES(3, 128, false)
+  UGEMM_SPLIT_CASES(2, 256, false)
+  UGEMM_SPLIT_CASES(2, 128, false)
+  UGEMM_SPLIT_CASES(2, 256, true)
+  UGEMM_SPLIT_CASES(2, 128, true)
 #undef UGEMM_SPLIT_CASES
 #undef UGEMM_SPLIT_CASE
   return UGEMM_ERR_ARG;
@@ -1134,13 +1210,14 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
     operand_max_batched_kernel<<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
     prof_end(st, kProfSplitPrep);
     prof_begin(st);
-    split_pieces_batched_kernel<2, true><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+    split_pieces_batched_kernel<2, 1><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
     prof_end(st, kProfSplitPrep);
     return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
   }
   prof_begin(st);
-  if (pieces == 3) split_pieces_batched_kernel<3, false><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
-  else split_pieces_batched_kernel<2, false><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  if (pieces == 3) split_pieces_batched_kernel<3, 0><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  else if (pieces == kPiecesTf32) split_pieces_batched_kernel<2, 2><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  else split_pieces_batched_kernel<2, 0><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
   prof_end(st, kProfSplitPrep);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
@@ -1151,8 +1228,8 @@ int split_kp(int K) { return kp_of(K); }
 
 namespace ugemm {
 
-// Split one operand (element (r, k) at src[r*sr + k*sk]) into `pieces` bf16
-// planes [pieces][rows][Kp] at dst.
+// Split one operand (element (r, k) at src[r*sr + k*sk]) into its planes
+// [planes][rows][Kp] of pieces at dst (layout code `pieces`).
 ugemm_status split_operand_launch(int pieces, const float* src, long long sr, long long sk,
                                   int rows, int K, void* dst, cudaStream_t st, bool f16) {
   const int Kp = kp_of(K);
@@ -1187,11 +1264,13 @@ ugemm_status split_operand_launch(int pieces, const float* src, long long sr, lo
       }
       prof_end(st, kProfSplitPrep);
     }
-    launch_split<2>(src, sr, sk, rows, K, Kp, d, st, words);
+    launch_split<2, 1>(src, sr, sk, rows, K, Kp, d, st, words);
   } else if (pieces == 3) {
-    launch_split<3>(src, sr, sk, rows, K, Kp, d, st);
+    launch_split<3, 0>(src, sr, sk, rows, K, Kp, d, st);
+  } else if (pieces == kPiecesTf32) {
+    launch_split<2, 2>(src, sr, sk, rows, K, Kp, d, st);
   } else {
-    launch_split<2>(src, sr, sk, rows, K, Kp, d, st);
+    launch_split<2, 0>(src, sr, sk, rows, K, Kp, d, st);
   }
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
@@ -1209,7 +1288,7 @@ ugemm_status split_gemm_on_pieces(const Gemm& g, const SplitPlan& p, const void*
     P.fmax_b = split_fmax_word(b_pieces, 2, g.N, g.K);
   }
   const int chunk =
-      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb());
+      split_chunk_stages(p.pieces, p.chunk_kb > 0 ? p.chunk_kb : split_default_chunk_kb(g.K));
   // a partial last wave of tiles runs as two k slices (multi.cu)
   const TailPlan tail = tail_scratch ? tail_plan(g, p) : TailPlan{};
   ugemm_status s = split_gemm_launch(p, ta, tb, P, nullptr, nullptr, nullptr,

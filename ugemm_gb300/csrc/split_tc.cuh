@@ -129,7 +129,7 @@ struct TcProblem {
 struct SplitJob {
   const float* src;
   long long sr, sk;     // element (r, k) at src[r*sr + k*sk]
-  __nv_bfloat16* dst;   // [pieces][rows][Kp]
+  __nv_bfloat16* dst;   // [planes][rows][Kp] pieces (32-bit ones for TF32 jobs)
   int rows, K, Kp;
   int tile_start;       // first 32x64 tile index of this job
   // implicit im2col operand (src unused): 1 = rows are pixels and k taps,
@@ -143,7 +143,7 @@ struct SplitJob {
 };
 
 int split_kp(int K);
-int split_default_chunk_kb();
+int split_default_chunk_kb(int K);
 // Bytes of one operand's pieces [pieces][rows][Kp]; two-piece operands also
 // carry a trailer of one word per row (rounded up to 256 bytes) that holds
 // the row's largest magnitude (split_fmax_word), used by the FP16x3 form.
@@ -151,10 +151,20 @@ size_t split_operand_bytes(int pieces, int rows, int K);
 unsigned* split_fmax_word(const void* pieces_base, int pieces, int rows, int K);
 void split_operand_strides(const Gemm& g, long long* a_sr, long long* a_sk, long long* b_sr,
                            long long* b_sk);
-// k depth of one pipeline stage: 64 for two-piece operands (128-byte
-// swizzle), 32 for three-piece ones (64-byte swizzle).  The tensor maps'
-// boxes and every launch's TcProblem::nkb follow it.
-constexpr int split_stage_k(int pieces) { return pieces == 2 ? 2 * kTcKB : kTcKB; }
+// Piece layouts, by the code that SplitPlan::pieces and the functions below
+// take: 3 = three 16-bit pieces (BF16x6/x9), 2 = two 16-bit pieces (BF16x3,
+// FP16x3), kPiecesTf32 = two 32-bit TF32 pieces (TF32x3).
+constexpr int kPiecesTf32 = 4;
+constexpr int piece_planes(int code) { return code == kPiecesTf32 ? 2 : code; }
+constexpr int piece_bytes(int code) { return code == kPiecesTf32 ? 4 : 2; }
+// The GEMM kernel instantiation a layout runs on: TF32 stages have the
+// shape of the two-piece 16-bit ones (two planes of 128-byte rows).
+constexpr int kernel_np(int code) { return code == kPiecesTf32 ? 2 : code; }
+// k depth of one pipeline stage: 64 for two 16-bit pieces and 32 for TF32
+// pieces (128-byte rows, 128-byte swizzle), 32 for three 16-bit pieces
+// (64-byte rows, 64-byte swizzle).  The tensor maps' boxes and every
+// launch's TcProblem::nkb follow it.
+constexpr int split_stage_k(int code) { return code == 2 ? 2 * kTcKB : kTcKB; }
 // Stages of the kernel's depth over K, and a chunk of `chunk_kb` 32-deep
 // k-blocks in stages.
 inline int split_nkb(int pieces, int K) {
