@@ -359,7 +359,8 @@ UGEMM_API int ugemm_sgemv(char trans, int M, int N, float alpha, const float *A,
  * synchronises, returns the summed milliseconds and launch counts per kind
  * (0 SIMT GEMM, 1 split pre-pass, 2 split tcgen05 GEMM, 3 auxiliary, 4 grouped
  * GEMM, 5 control: the one-thread error-word fold that starts each
- * device-pointer call) and clears the record. */
+ * device-pointer call, 6 copy: the copy kernels that read pageable host
+ * buffers) and clears the record. */
 UGEMM_API int ugemm_profile_enable(int on);
 UGEMM_API int ugemm_profile_collect(double *ms_per_kind, int *launches_per_kind, int nkinds);
 

@@ -57,7 +57,7 @@ EXPORTS = (
     "ugemm_sgemm_grouped", "ugemm_tune_grouped", "ugemm_check", "ugemm_dgemm_oracle_dev",
     "ugemm_sgemm_dev_noalloc", "ugemm_debug_set_error_word",
 )
-PROF_KINDS = ("simt", "split_prepass", "split_gemm", "aux", "grouped", "control")
+PROF_KINDS = ("simt", "split_prepass", "split_gemm", "aux", "grouped", "control", "copy")
 
 
 class UgemmError(RuntimeError):

@@ -247,7 +247,7 @@ namespace ugemm {
 // Optional per-kernel timing (CUDA events on the launching stream), enabled by
 // ugemm_profile_enable; used by the benchmark to attribute time to kernels.
 enum ProfKind : int { kProfSimt = 0, kProfSplitPrep = 1, kProfSplitGemm = 2, kProfAux = 3,
-                      kProfGrouped = 4, kProfControl = 5, kProfKinds = 6 };
+                      kProfGrouped = 4, kProfControl = 5, kProfCopy = 6, kProfKinds = 7 };
 void prof_begin(cudaStream_t st);
 void prof_end(cudaStream_t st, int kind);
 }  // namespace ugemm

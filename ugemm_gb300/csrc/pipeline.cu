@@ -157,8 +157,10 @@ bool copy2d_launch(void* dst, size_t dpitch, const void* src, size_t spitch, siz
   const int grid = std::min(rows, copy_ctas());
   const bool vec = ((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d) | spitch |
                      dpitch | width) & 15) == 0;
+  prof_begin(st);
   if (vec) copy2d_kernel<float4><<<grid, 256, 0, st>>>(s, spitch, d, dpitch, width, rows);
   else copy2d_kernel<float><<<grid, 256, 0, st>>>(s, spitch, d, dpitch, width, rows);
+  prof_end(st, kProfCopy);
   return cudaPeekAtLastError() == cudaSuccess;
 }
 
