@@ -29,25 +29,30 @@
 //
 // Host buffers.  The reference's callers pass pageable memory (sgemm_test.c
 // declares `static float A[...]` and hands it to sgemm_ocl, whose oclWrite
-// copies it, sgemm_ocl2.h:173-176).  A cudaMemcpyAsync from pageable memory
-// returns only when the copy is done, which would serialise every copy and
-// launch behind it.  Where the device can address pageable memory itself
-// (a Grace host: NVLink-C2C with address translation; measured 201 GB/s of
-// kernel reads against 210 GB/s pinned copies), the reads of pageable
-// buffers -- A, B and the incoming C, whose pages hold the caller's data --
-// are stream-ordered copy kernels on the copy streams (a few dozen CTAs,
-// which fit beside a running GEMM's); the bands of C go back with the copy
-// engines, enqueued after every GEMM of the call, so that a copy that
-// returns only when done costs no overlap.  Where the device cannot address
-// pageable memory, the call registers the buffers' ranges for its duration
-// (cudaHostRegister) so that the copy engines run every copy asynchronously.
-// Pinned buffers use the copy engines.
+// copies it, sgemm_ocl2.h:173-176).  A cudaMemcpyAsync from or to pageable
+// memory returns only when the copy is done, which in one host thread would
+// serialise every copy and launch behind it.  So when a buffer is pageable
+// the copies run from two helper host threads -- the copies in, in the order
+// the GEMMs need them, and the bands of C back, each as soon as its GEMM is
+// done -- while this thread launches: before a launch that needs a copy it
+// waits for that copy only.  The copy engines move pageable memory nearly as
+// fast as pinned memory (GB300 with a Grace host, measured: 184-196 GB/s
+// in, 191 GB/s out, against 210 and 192 pinned).  Two alternatives were
+// measured at 8192^3 and are kept behind UGEMM_PAGEABLE: copy kernels that
+// read pageable memory through the host link's address translation
+// ("kernel": 203 GB/s alone, but beside the GEMMs they ran at 121 GB/s and
+// slowed the GEMMs by a quarter: 161 TFLOPS end to end) and registering the
+// buffers for the call ("register": 1.9 ms of page pinning per call, 168
+// TFLOPS), against 239 with pinned buffers.  Pinned buffers use the copy
+// engines from this thread.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -179,10 +184,12 @@ bool device_reads_pageable() {
   return cached[dev] != 0;
 }
 
-// How the copies of one host buffer cross the link: the copy engines (pinned
-// or registered memory), copy kernels (reads of pageable memory the device
-// addresses), or the copy engines after registering the buffer for the call.
-enum class Xfer { kEngine, kKernel, kRegistered };
+// How the copies of one host buffer cross the link: the copy engines from
+// this thread (pinned or registered memory), the copy engines from a helper
+// thread (pageable memory: the copy returns when done), copy kernels (reads
+// of pageable memory the device addresses), or the copy engines after
+// registering the buffer for the call.
+enum class Xfer { kEngine, kThread, kKernel, kRegistered };
 
 bool is_pageable(const void* p) {
   cudaPointerAttributes a;
@@ -204,14 +211,13 @@ struct Registrations {
   }
 };
 
-// UGEMM_PAGEABLE selects how pageable buffers travel where the device
-// addresses them: "kernel" (the default: reads by copy kernels, C back by the
-// copy engines), "kernel_all" (C back by a copy kernel too) or "register"
-// (every buffer registered for the call, all copies by the copy engines).
+// UGEMM_PAGEABLE selects how pageable buffers travel: "threads" (the
+// default), "kernel" (reads by copy kernels where the device addresses
+// pageable memory) or "register".
 int pageable_mode() {
   static const int m = [] {
     const char* e = std::getenv("UGEMM_PAGEABLE");
-    if (e && std::strcmp(e, "kernel_all") == 0) return 1;
+    if (e && std::strcmp(e, "kernel") == 0) return 1;
     if (e && std::strcmp(e, "register") == 0) return 2;
     return 0;
   }();
@@ -220,16 +226,99 @@ int pageable_mode() {
 
 Xfer xfer_for(const void* p, size_t bytes, Registrations& regs) {
   if (!p || bytes == 0 || !is_pageable(p)) return Xfer::kEngine;
-  if (device_reads_pageable() && pageable_mode() != 2) return Xfer::kKernel;
-  void* q = const_cast<void*>(p);
-  if (cudaHostRegister(q, bytes, cudaHostRegisterDefault) == cudaSuccess) {
-    regs.ptrs.push_back(q);
-    return Xfer::kRegistered;
+  if (pageable_mode() == 1 && device_reads_pageable()) return Xfer::kKernel;
+  if (pageable_mode() == 2) {
+    void* q = const_cast<void*>(p);
+    if (cudaHostRegister(q, bytes, cudaHostRegisterDefault) == cudaSuccess) {
+      regs.ptrs.push_back(q);
+      return Xfer::kRegistered;
+    }
+    (void)cudaGetLastError();
   }
-  (void)cudaGetLastError();
-  return Xfer::kEngine;  // pageable copies that return when done: correct, not overlapped
+  return Xfer::kThread;
 }
 
+// A host thread that runs numbered steps in order (each may block) and
+// counts the ones done; other threads wait for a given step.  Stopping makes
+// waits fail and the thread finish after its current step.  Joined on
+// destruction, so it never outlives the buffers its steps use.
+class StepThread {
+ public:
+  ~StepThread() { stop(); }
+  template <typename Step>
+  void start(int n, Step step) {
+    th_ = std::thread([this, n, step] {
+      for (int i = 0; i < n; ++i) {
+        if (stopped() || !step(i)) {
+          std::lock_guard<std::mutex> l(mu_);
+          failed_ = true;
+          cv_.notify_all();
+          return;
+        }
+        std::lock_guard<std::mutex> l(mu_);
+        done_ = i + 1;
+        cv_.notify_all();
+      }
+    });
+  }
+  bool wait(int i) {  // step i done; false if the thread failed or stopped first
+    std::unique_lock<std::mutex> l(mu_);
+    cv_.wait(l, [&] { return done_ > i || failed_ || stop_; });
+    return done_ > i;
+  }
+  bool join() {  // all steps ran
+    if (th_.joinable()) th_.join();
+    std::lock_guard<std::mutex> l(mu_);
+    return !failed_;
+  }
+  void stop() {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      stop_ = true;
+      cv_.notify_all();
+    }
+    if (th_.joinable()) th_.join();
+  }
+
+ private:
+  bool stopped() {
+    std::lock_guard<std::mutex> l(mu_);
+    return stop_;
+  }
+  std::thread th_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  int done_ = 0;
+  bool failed_ = false, stop_ = false;
+};
+
+// A count that one thread raises and another waits on (launches recorded).
+class Counter {
+ public:
+  void raise(int n) {
+    std::lock_guard<std::mutex> l(mu_);
+    n_ = n;
+    cv_.notify_all();
+  }
+  void abort() {
+    std::lock_guard<std::mutex> l(mu_);
+    aborted_ = true;
+    cv_.notify_all();
+  }
+  bool wait(int n) {
+    std::unique_lock<std::mutex> l(mu_);
+    cv_.wait(l, [&] { return n_ >= n || aborted_; });
+    return n_ >= n;
+  }
+
+ private:
+  std::mutex mu_;
+  std::condition_variable cv_;
+  int n_ = 0;
+  bool aborted_ = false;
+};
+
+// (kThread copies are issued like kEngine ones, from the helper thread)
 bool copy2d(Xfer x, void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
             int rows, cudaMemcpyKind kind, cudaStream_t st) {
   if (x == Xfer::kKernel) return copy2d_launch(dst, dpitch, src, spitch, width, rows, st);
@@ -383,8 +472,11 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   const size_t c_span = (size_t(g.M) - 1) * g.ldc + g.N;
   const Xfer xa = xfer_for(g.A, a_span * 4, regs), xb = xfer_for(g.B, b_span * 4, regs);
   const Xfer xc = xfer_for(g.C, c_span * 4, regs);
-  const Xfer xc_out =  // C goes back by the copy engines unless asked otherwise
-      xc == Xfer::kKernel && pageable_mode() != 1 ? Xfer::kEngine : xc;
+  // copies from or into pageable memory that return when done run in helper
+  // threads (C goes back that way also when copy kernels read it in)
+  const bool in_threaded = xa == Xfer::kThread || xb == Xfer::kThread ||
+                           (g.beta != 0.f && xc == Xfer::kThread);
+  const bool out_threaded = xc == Xfer::kThread || xc == Xfer::kKernel;
   uint8_t* base = static_cast<uint8_t*>(arena);
   size_t off = 0;
   auto take = [&](size_t n) { uint8_t* p = base + off; off += n; return p; };
@@ -404,21 +496,37 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   }
   auto ck = [](cudaError_t e) { return e == cudaSuccess; };
 
+  // The copies in, as a list in the order the GEMMs consume them; the last
+  // copy of each group records the group's event.
+  struct CopyIn {
+    Xfer x;
+    void* dst;
+    size_t dpitch;
+    const void* src;
+    size_t spitch, width;
+    int rows;
+    cudaEvent_t after;
+  };
+  std::vector<CopyIn> ins;
   // a region of op(A) (rows m0.., k0..) or op(B) (k0.., columns n0..) from
   // the host operand into the same place of the device copy
   auto copy_a = [&](int m0, int mr, int k0, int kw) {
     const int r0 = g.ta == 'N' ? m0 : k0, c0 = g.ta == 'N' ? k0 : m0;
     const int nr = g.ta == 'N' ? mr : kw, nc = g.ta == 'N' ? kw : mr;
-    return copy2d(xa, dA + size_t(r0) * lda_d + c0, size_t(lda_d) * 4,
-                  g.A + size_t(r0) * g.lda + c0, size_t(g.lda) * 4, size_t(nc) * 4, nr,
-                  cudaMemcpyHostToDevice, ps->h2d);
+    ins.push_back(CopyIn{xa, dA + size_t(r0) * lda_d + c0, size_t(lda_d) * 4,
+                         g.A + size_t(r0) * g.lda + c0, size_t(g.lda) * 4, size_t(nc) * 4, nr,
+                         nullptr});
   };
   auto copy_b = [&](int k0, int kw) {  // all N columns of op(B), k rows k0..k0+kw
     const int r0 = g.tb == 'N' ? k0 : 0, c0 = g.tb == 'N' ? 0 : k0;
     const int nr = g.tb == 'N' ? kw : g.N, nc = g.tb == 'N' ? g.N : kw;
-    return copy2d(xb, dB + size_t(r0) * ldb_d + c0, size_t(ldb_d) * 4,
-                  g.B + size_t(r0) * g.ldb + c0, size_t(g.ldb) * 4, size_t(nc) * 4, nr,
-                  cudaMemcpyHostToDevice, ps->h2d);
+    ins.push_back(CopyIn{xb, dB + size_t(r0) * ldb_d + c0, size_t(ldb_d) * 4,
+                         g.B + size_t(r0) * g.ldb + c0, size_t(g.ldb) * 4, size_t(nc) * 4, nr,
+                         nullptr});
+  };
+  auto close_group = [&](cudaEvent_t e) {
+    ins.back().after = e;
+    return static_cast<int>(ins.size()) - 1;
   };
   auto a_view = [&](int m0, int k0) { return dA + m0 * a_sr + k0 * a_sk; };
   auto b_view = [&](int k0) { return dB + k0 * b_sk; };
@@ -429,26 +537,63 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
     if (!ck(cudaStreamWaitEvent(s, ps->entry, 0))) return UGEMM_ERR_CUDA;
 
   // ---- copies in, in the order the GEMMs consume them
+  std::vector<int> slab_in_op(L.nslab), band_in_op(L.nband);
   for (int i = 0; i < L.nslab; ++i) {
-    const int k0 = L.slab_k0[i], w = L.slab_w[i];
-    if (!copy_a(0, g.M, k0, w) || !copy_b(k0, w) || !ck(cudaEventRecord(ps->slab_in[i], ps->h2d)))
-      return UGEMM_ERR_CUDA;
+    copy_a(0, g.M, L.slab_k0[i], L.slab_w[i]);
+    copy_b(L.slab_k0[i], L.slab_w[i]);
+    slab_in_op[i] = close_group(ps->slab_in[i]);
   }
-  if (!copy_b(k1, k2) || !ck(cudaEventRecord(ps->rest_in, ps->h2d))) return UGEMM_ERR_CUDA;
+  copy_b(k1, k2);
+  const int rest_in_op = close_group(ps->rest_in);
   for (int r = 0; r < L.nband; ++r) {
     const int m0 = L.band_m0[r], mb = L.band_h[r];
-    if (!copy_a(m0, mb, k1, k2)) return UGEMM_ERR_CUDA;
-    if (g.beta != 0.f &&  // beta == 0: C is not read (sgemm_ocl2.h:177)
-        !copy2d(xc, dCin + size_t(m0) * ldc_d, size_t(ldc_d) * 4, g.C + size_t(m0) * g.ldc,
-                size_t(g.ldc) * 4, size_t(g.N) * 4, mb, cudaMemcpyHostToDevice, ps->h2d))
-      return UGEMM_ERR_CUDA;
-    if (!ck(cudaEventRecord(ps->band_in[r], ps->h2d))) return UGEMM_ERR_CUDA;
+    copy_a(m0, mb, k1, k2);
+    if (g.beta != 0.f)  // beta == 0: C is not read (sgemm_ocl2.h:177)
+      ins.push_back(CopyIn{xc, dCin + size_t(m0) * ldc_d, size_t(ldc_d) * 4,
+                           g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, size_t(g.N) * 4, mb,
+                           nullptr});
+    band_in_op[r] = close_group(ps->band_in[r]);
   }
+  auto run_in = [&](int i) {
+    const CopyIn& o = ins[i];
+    return copy2d(o.x, o.dst, o.dpitch, o.src, o.spitch, o.width, o.rows, cudaMemcpyHostToDevice,
+                  ps->h2d) &&
+           (!o.after || ck(cudaEventRecord(o.after, ps->h2d)));
+  };
+  // the helpers are declared after everything their steps use (the counter
+  // included), so they are joined first on every return; the guard declared
+  // last releases a drainer still waiting for a band that an error return
+  // will never launch
+  Counter bands_launched;
+  StepThread feeder, drainer;
+  struct AbortOnExit {
+    Counter& c;
+    ~AbortOnExit() { c.abort(); }
+  } abort_drain{bands_launched};
+  if (in_threaded) {
+    feeder.start(static_cast<int>(ins.size()), run_in);
+  } else {
+    for (int i = 0; i < static_cast<int>(ins.size()); ++i)
+      if (!run_in(i)) return UGEMM_ERR_CUDA;
+  }
+  // before a launch that waits on a group's event: that event is recorded
+  auto await_in = [&](int op) { return !in_threaded || feeder.wait(op); };
+  // the bands of C back to the host, each once its GEMM is done
+  auto run_out = [&](int r) {
+    const int m0 = L.band_m0[r], mb = L.band_h[r];
+    const Xfer x = out_threaded ? Xfer::kEngine : xc;
+    return ck(cudaStreamWaitEvent(ps->d2h, ps->band_done[r], 0)) &&
+           copy2d(x, g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, dC + size_t(m0) * ldc_d,
+                  size_t(ldc_d) * 4, size_t(g.N) * 4, mb, cudaMemcpyDeviceToHost, ps->d2h);
+  };
+  if (out_threaded)
+    drainer.start(L.nband, [&](int r) { return bands_launched.wait(r + 1) && run_out(r); });
 
   // ---- phase 1: slab GEMMs into the accumulator dC, one after another
   cudaStream_t g0 = ps->gemm[0];
   for (int i = 0; i < L.nslab; ++i) {
     const int k0 = L.slab_k0[i], w = L.slab_w[i];
+    if (!await_in(slab_in_op[i])) return UGEMM_ERR_CUDA;
     if (split) {
       cudaStreamWaitEvent(ps->prep, ps->slab_in[i], 0);
       if (split_operand_launch(L.plan.pieces, a_view(0, k0), a_sr, a_sk, g.M, w, sap[i], ps->prep,
@@ -477,6 +622,7 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   if (!ck(cudaEventRecord(ps->acc_done, g0))) return UGEMM_ERR_CUDA;
 
   // ---- phase 2: the rest of op(B), then band by band
+  if (!await_in(rest_in_op)) return UGEMM_ERR_CUDA;
   cudaStreamWaitEvent(ps->prep, ps->rest_in, 0);
   if (split && split_operand_launch(L.plan.pieces, b_view(k1), b_sr, b_sk, g.N, k2, rbp,
                                     ps->prep, L.plan.f16) != UGEMM_OK)
@@ -485,6 +631,7 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
   for (int r = 0; r < L.nband; ++r) {
     const int m0 = L.band_m0[r], mb = L.band_h[r];
     cudaStream_t gs_st = ps->gemm[r & 1];
+    if (!await_in(band_in_op[r])) return UGEMM_ERR_CUDA;
     cudaStreamWaitEvent(ps->prep, ps->band_in[r], 0);
     if (split && split_operand_launch(L.plan.pieces, a_view(m0, k1), a_sr, a_sk, mb, k2, bap[r],
                                       ps->prep, L.plan.f16) != UGEMM_OK)
@@ -515,17 +662,16 @@ ugemm_status host_gemm_pipelined(const Gemm& g, int form, void* arena, size_t ar
                             : simt_launch(gb, simt_pick_tile(gb), Scratch{nullptr, 0}, dev_err,
                                           gs_st);
     if (st != UGEMM_OK || !ck(cudaEventRecord(ps->band_done[r], gs_st))) return UGEMM_ERR_CUDA;
+    bands_launched.raise(r + 1);
   }
   // ---- finished bands back to the host, each as soon as its GEMM is done
-  // (enqueued after all the GEMMs: a copy into pageable memory returns only
-  // when done)
-  for (int r = 0; r < L.nband; ++r) {
-    const int m0 = L.band_m0[r], mb = L.band_h[r];
-    cudaStreamWaitEvent(ps->d2h, ps->band_done[r], 0);
-    if (!copy2d(xc_out, g.C + size_t(m0) * g.ldc, size_t(g.ldc) * 4, dC + size_t(m0) * ldc_d,
-                size_t(ldc_d) * 4, size_t(g.N) * 4, mb, cudaMemcpyDeviceToHost, ps->d2h))
-      return UGEMM_ERR_CUDA;
+  if (out_threaded) {
+    if (!drainer.join()) return UGEMM_ERR_CUDA;
+  } else {
+    for (int r = 0; r < L.nband; ++r)
+      if (!run_out(r)) return UGEMM_ERR_CUDA;
   }
+  if (in_threaded && !feeder.join()) return UGEMM_ERR_CUDA;
   // the caller's stream resumes after the last copy back
   if (!ck(cudaEventRecord(ps->last_out, ps->d2h))) return UGEMM_ERR_CUDA;
   cudaStreamWaitEvent(caller, ps->last_out, 0);
