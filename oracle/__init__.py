@@ -36,11 +36,13 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref() -> bool:
-    """Compile the reference's own CPU GEMMs (x86-64 with the reference tree only)."""
+def build_ref(ref_dir: str | None = None) -> bool:
+    """Compile the reference's own CPU GEMMs (x86-64 with the reference tree
+    only) from `ref_dir`, else from $UGEMM_REF_DIR; False if neither names a
+    directory."""
     import platform
-    ref_dir = os.environ.get("UGEMM_REF_DIR", "/root/reference")
-    if platform.machine() != "x86_64" or not os.path.isdir(ref_dir):
+    ref_dir = ref_dir or os.environ.get("UGEMM_REF_DIR")
+    if platform.machine() != "x86_64" or not ref_dir or not os.path.isdir(ref_dir):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True)
     return True

@@ -16,7 +16,7 @@ calls the reference functions through ctypes:
 
 Inputs are drawn from numpy's PCG64 with fixed seeds and stored beside the
 outputs, so the fixture file alone is enough on a machine without the
-reference.  Usage: ``python tests/golden/make_golden.py``.
+reference.  Usage: ``python tests/golden/make_golden.py <reference tree>``.
 """
 from __future__ import annotations
 
@@ -62,8 +62,10 @@ def capture_stdout(fn):
 
 
 def main() -> None:
-    if not oracle.build_ref():
-        raise SystemExit("the reference tree (x86-64) is needed to make the golden file")
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else None
+    if not oracle.build_ref(ref_dir):
+        raise SystemExit("usage: make_golden.py <reference tree> (or set UGEMM_REF_DIR; "
+                         "x86-64 only)")
     strict = oracle.load_ref(fast=False)
     fast = oracle.load_ref(fast=True)
     rng = np.random.default_rng(20261203)
