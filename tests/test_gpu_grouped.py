@@ -21,15 +21,21 @@ def gpu():
     ug.load()
 
 
-def make_group(shapes, seed=1, alpha=1.0, beta=0.0, pad=0):
+def make_group(shapes, seed=1, alpha=1.0, beta=0.0, pad=0, align=1):
+    """Problems with leading dimensions of (columns + pad) rounded up to a
+    multiple of align."""
     g = torch.Generator(device="cuda").manual_seed(seed)
     specs, refs = [], []
+
+    def ld(cols):
+        return -(-(cols + pad) // align) * align
+
     for (ta, tb, M, N, K) in shapes:
         ashape = (M, K) if ta == "N" else (K, M)
         bshape = (K, N) if tb == "N" else (N, K)
-        A = torch.rand((ashape[0], ashape[1] + pad), device="cuda", generator=g) * 2 - 1
-        B = torch.rand((bshape[0], bshape[1] + pad), device="cuda", generator=g) * 2 - 1
-        C = torch.rand((M, N + pad), device="cuda", generator=g) * 2 - 1
+        A = torch.rand((ashape[0], ld(ashape[1])), device="cuda", generator=g) * 2 - 1
+        B = torch.rand((bshape[0], ld(bshape[1])), device="cuda", generator=g) * 2 - 1
+        C = torch.rand((M, ld(N)), device="cuda", generator=g) * 2 - 1
         a = A[:, :ashape[1]].double()
         b = B[:, :bshape[1]].double()
         ref = alpha * ((a if ta == "N" else a.T) @ (b if tb == "N" else b.T)) + beta * C[:, :N].double()
@@ -167,13 +173,13 @@ def test_autotuner_caches_its_choice(tmp_path, monkeypatch):
     # searched (split-K threshold, tile deal, transposed tiles, grid size),
     # and the choice is the fastest of them
     cands = line["candidates"]
-    fields = ("block_n", "chunk_k", "max_ctas", "split_k", "deal", "transpose")
-    assert len(cands) >= 9
+    fields = ("block_n", "chunk_k", "max_ctas", "split_k", "deal", "transpose", "fused")
+    assert len(cands) >= 11
     for i, name in enumerate(fields[2:], start=2):
         assert len({c[i] for c in cands}) >= 2, name
-    fastest = min(cands, key=lambda c: c[6])
-    assert fastest[6] == pytest.approx(line["ms"], rel=1e-6)
-    assert dict(zip(fields, fastest[:6])) == best
+    fastest = min(cands, key=lambda c: c[7])
+    assert fastest[7] == pytest.approx(line["ms"], rel=1e-6)
+    assert dict(zip(fields, fastest[:7])) == best
     # cached: returned without timing, and picked up by a plan without config
     again, ms2 = ug.tune_grouped(specs, precision="bf16x6")
     assert again == best and ms2 == pytest.approx(ms, rel=1e-5)
@@ -186,4 +192,4 @@ def test_autotuner_caches_its_choice(tmp_path, monkeypatch):
     simt_best, _ = ug.tune_grouped(specs, precision="simt", force=True)
     assert simt_best["block_n"] in (64, 128)
     simt_line = json.loads(cache.read_text().splitlines()[-1])
-    assert min(c[6] for c in simt_line["candidates"]) == pytest.approx(simt_line["ms"], rel=1e-6)
+    assert min(c[7] for c in simt_line["candidates"]) == pytest.approx(simt_line["ms"], rel=1e-6)

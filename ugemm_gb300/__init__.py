@@ -358,7 +358,7 @@ class Problem(ctypes.Structure):
 class TileConfig(ctypes.Structure):
     """ugemm_tile_config: tile shape and schedule of a grouped launch."""
     _fields_ = [("block_n", _i), ("chunk_k", _i), ("max_ctas", _i), ("split_k", _i),
-                ("deal", _i), ("transpose", _i)]
+                ("deal", _i), ("transpose", _i), ("fused", _i)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -109,9 +109,11 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
                             p->gemm_tiles, p->cfg.max_ctas, p->dev_err, st);
     return s == UGEMM_OK ? reduce_launch(p, st) : s;
   }
-  s = split_batched_launch(p->split.pieces, static_cast<const SplitJob*>(p->jobs), p->njobs,
-                           p->prep_tiles, st, p->fmax, p->nfmax);
-  if (s != UGEMM_OK) return s;
+  if (!p->split.fused) {
+    s = split_batched_launch(p->split.pieces, static_cast<const SplitJob*>(p->jobs), p->njobs,
+                             p->prep_tiles, st, p->fmax, p->nfmax);
+    if (s != UGEMM_OK) return s;
+  }
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
@@ -120,6 +122,34 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
                         split_chunk_stages(p->split.pieces, std::max(1, p->cfg.chunk_k / kTcKB)),
                         p->grid, p->dev_err, st);
   return s == UGEMM_OK ? reduce_launch(p, st) : s;
+}
+
+// The FP32 source of one kernel operand of a fused launch (rows of op(A),
+// or of op(B)^T, by k) as a 2-D tensor map: k contiguous (row stride sr) or
+// rows contiguous (k stride sk).  *kc says which.
+bool fused_operand_map(const float* base, long long sr, long long sk, int rows, int K,
+                       int box_rows, CUtensorMap* map, int* kc) {
+  if (sk == 1) {
+    *kc = 1;
+    return fused_encode_map(base, sr, rows, K, true, box_rows, map);
+  }
+  *kc = 0;
+  return sr == 1 && fused_encode_map(base, sk, K, rows, false, box_rows, map);
+}
+
+// A fused launch copies the FP32 operands with TMA: each needs a unit
+// stride, a 16-byte aligned base and leading dimension, and k > 0 (a K == 0
+// problem's operands may be empty); implicit im2col gathers take the
+// pre-pass.
+bool fusable(const Gemm& x) {
+  if (x.K == 0 || x.b_im2col) return false;
+  long long a_sr, a_sk, b_sr, b_sk;
+  split_operand_strides(x, &a_sr, &a_sk, &b_sr, &b_sk);
+  auto ok = [](const float* p, long long sr, long long sk) {
+    const long long ld = sk == 1 ? sr : sk;
+    return (sr == 1 || sk == 1) && (reinterpret_cast<uintptr_t>(p) & 15) == 0 && ld % 4 == 0;
+  };
+  return ok(x.A, a_sr, a_sk) && ok(x.B, b_sr, b_sk);
 }
 
 // Padded tile area of an R x C output in 128 x bn tiles whose right-edge
@@ -226,10 +256,17 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
     }
   }
   if (form != UGEMM_PREC_SIMT) {
+    // fused launches split three bf16 pieces inside the GEMM kernel, with
+    // 128-wide tiles; other forms ignore the knob
+    const bool can_fuse = split_plan_for(form, g[0]).pieces == 3 &&
+                          std::all_of(g.begin(), g.end(), fusable);
+    if (p->cfg.fused && can_fuse) p->cfg.block_n = 128;
+    else p->cfg.fused = 0;
     if (p->cfg.block_n != 128 && p->cfg.block_n != 256) p->cfg.block_n = 256;
     if (p->cfg.chunk_k < kTcKB) p->cfg.chunk_k = split_default_chunk_kb(1 << 30) * kTcKB;
-  } else if (p->cfg.block_n != 64 && p->cfg.block_n != 128) {
-    p->cfg.block_n = 128;
+  } else {
+    p->cfg.fused = 0;
+    if (p->cfg.block_n != 64 && p->cfg.block_n != 128) p->cfg.block_n = 128;
   }
   cudaGetDevice(&p->device);
   int sms = 148;
@@ -242,6 +279,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   if (!simt) {
     p->split = split_plan_for(form, g[0]);
     p->split.block_n = bn;
+    p->split.fused = p->cfg.fused != 0;
     pieces = p->split.pieces;
   }
   // Kernel geometry of each problem (in k-depth order j).  The split form
@@ -313,6 +351,8 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
       scratch += align_up(size_t(std::max(x.K, 1)) * ld_a[j] * 4, 256);
       b_off[j] = scratch;
       scratch += align_up(size_t(std::max(x.K, 1)) * ld_b[j] * 4, 256);
+    } else if (p->split.fused) {
+      b_off[j] = scratch;  // no pieces in memory: the kernel splits the operands
     } else {
       scratch += split_operand_bytes(pieces, x.M, x.K);
       b_off[j] = scratch;
@@ -409,13 +449,26 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
       tiles += sp.tiles_m * sp.tiles_n;
       sprobs.push_back(sp);
     } else {
-      const void* da = base + a_off[u.j];
-      const void* db = base + b_off[u.j];
-      ok = o.swap ? split_encode_maps(pieces, bn, db, x.N, da, x.M, x.K, &maps[2 * i],
-                                      &maps[2 * i + 1])
-                  : split_encode_maps(pieces, bn, da, x.M, db, x.N, x.K, &maps[2 * i],
-                                      &maps[2 * i + 1]);
       TcProblem tp{};
+      if (p->split.fused) {
+        // the kernel copies the FP32 operands; its operand a is op(B)^T
+        // when the problem is computed transposed
+        long long a_sr, a_sk, b_sr, b_sk;
+        split_operand_strides(x, &a_sr, &a_sk, &b_sr, &b_sk);
+        ok = o.swap ? fused_operand_map(x.B, b_sr, b_sk, x.N, x.K, kTcBM, &maps[2 * i], &tp.kc_a) &&
+                          fused_operand_map(x.A, a_sr, a_sk, x.M, x.K, bn, &maps[2 * i + 1],
+                                            &tp.kc_b)
+                    : fused_operand_map(x.A, a_sr, a_sk, x.M, x.K, kTcBM, &maps[2 * i], &tp.kc_a) &&
+                          fused_operand_map(x.B, b_sr, b_sk, x.N, x.K, bn, &maps[2 * i + 1],
+                                            &tp.kc_b);
+      } else {
+        const void* da = base + a_off[u.j];
+        const void* db = base + b_off[u.j];
+        ok = o.swap ? split_encode_maps(pieces, bn, db, x.N, da, x.M, x.K, &maps[2 * i],
+                                        &maps[2 * i + 1])
+                    : split_encode_maps(pieces, bn, da, x.M, db, x.N, x.K, &maps[2 * i],
+                                        &maps[2 * i + 1]);
+      }
       tp.C = target;
       tp.M = o.swap ? x.N : x.M;
       tp.N = o.swap ? x.M : x.N;

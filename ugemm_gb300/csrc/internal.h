@@ -149,6 +149,9 @@ struct SplitPlan {
   bool f16 = false;  // FP16x3: scaled fp16 pieces (pieces == 2) instead of bf16
   bool epi = false;  // some problem carries a bias or activation: launch the
                      // kernel instantiation that has the fused epilogue
+  bool fused = false;  // grouped launches of three bf16 pieces, 128-wide
+                       // tiles: the GEMM kernel splits the FP32 operands
+                       // itself (no pre-pass, no pieces in memory)
 };
 
 // --- tensor maps -------------------------------------------------------

@@ -115,11 +115,23 @@ __device__ __forceinline__ TileCoord tile_coord(const TcProblem& single, const T
   return tc;
 }
 
+// The converter warps of a fused launch (defined with the split helpers).
+template <int NP, int BN>
+__device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
+                              uint8_t* pieces, uint8_t* raw, uint64_t* full, uint64_t* empty,
+                              uint64_t* raw_full, uint64_t* raw_empty, int ct, int* err);
+
 // TF32: the TF32x3 form's instantiation (two planes of 32-deep tf32
 // stages, tcgen05 kind::tf32), a template parameter so that the 16-bit
 // instantiations' MMA issue loop carries no branch on the format.
-template <int NP, int BN, bool GROUPED, bool EPI, bool TF32 = false>
-__global__ void __launch_bounds__(kTcThreads, 1)
+// FUSED (grouped launches of three bf16 pieces): instead of TMA copies of
+// pieces made by a pre-pass, TMA copies of the FP32 operand tiles land in a
+// raw ring, and converter warps split them and store the pieces into a
+// piece ring in the layout the piece copies would have had (K-major, 64-byte
+// rows, 64-byte swizzle), so the MMA issuer and the epilogue run unchanged
+// and the results are the same bits.
+template <int NP, int BN, bool GROUPED, bool EPI, bool TF32 = false, bool FUSED = false>
+__global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
     split_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
                     const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
@@ -129,19 +141,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // read two planes of 32-deep stages with the 128-byte rows of the
   // two-piece 16-bit shape
   static_assert(!TF32 || NP == 2, "TF32 pieces come in two planes");
+  static_assert(!FUSED || (NP == 3 && GROUPED && !TF32), "fused: grouped bf16x3-piece launches");
   constexpr bool WIDE = split_stage_k(NP) > kTcKB;
   using S = TcShape<NP, BN, WIDE>;
   constexpr int KB = S::KB;
   // K-major operand tiles: 8-row groups of 128-byte rows (128-byte swizzle)
   // or of 64-byte rows (64-byte swizzle); one k16 MMA step is 32 bytes
   constexpr uint32_t SBO = WIDE ? 1024 : 512, SWZ = WIDE ? 2 : 4;
+  // stages of pieces the MMA issuer reads; a fused launch's raw stages follow
+  constexpr int NST = FUSED ? kTcFusedPieceStages : S::STAGES;
+  constexpr int RST = FUSED ? kTcRawStages : 0;
+  constexpr size_t RING = FUSED ? S::FUSED_RING : size_t(S::STAGES) * S::STAGE_BYTES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S::STAGES * S::STAGE_BYTES);
-  uint64_t* empty = full + S::STAGES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + RING);
+  uint64_t* empty = full + NST;
+  uint64_t* raw_full = empty + NST;   // fused: a raw stage's copies landed
+  uint64_t* raw_empty = raw_full + RST;  // fused: the converters read it
   // one set per TMEM accumulator buffer (two when 2 x 2 x BN columns fit)
   constexpr int NB = S::ACC_BUFS;
-  uint64_t* main_full = empty + S::STAGES;   // a main-product chunk is complete
+  uint64_t* main_full = raw_empty + RST;   // a main-product chunk is complete
   uint64_t* main_empty = main_full + NB;     // the epilogue drained it
   uint64_t* tile_full = main_empty + NB;     // all MMAs of a tile are complete
   uint64_t* tmem_empty = tile_full + NB;     // the epilogue read both accumulators
@@ -149,9 +168,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < S::STAGES; ++s) {
-      mbar_init(&full[s], 1);
+    for (int s = 0; s < NST; ++s) {
+      // a fused piece stage is written by the converter threads, each of
+      // which arrives once its stores are visible to the tensor core
+      mbar_init(&full[s], FUSED ? kTcConvThreads : 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int s = 0; s < RST; ++s) {
+      mbar_init(&raw_full[s], 1);
+      mbar_init(&raw_empty[s], kTcConvThreads);
     }
     for (int b = 0; b < NB; ++b) {
       mbar_init(&main_full[b], 1);
@@ -170,7 +195,44 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
+  if (FUSED && warp >= 2 + kTcEpiWarps) {
+    // ------------------------------------------------- fused converters
+    if constexpr (FUSED)
+      fused_convert<NP, BN>(probs, tiles, smem, smem + NST * S::STAGE_BYTES, full, empty,
+                            raw_full, raw_empty, (warp - 2 - kTcEpiWarps) * 32 + lane, err);
+  } else if (FUSED && warp == 0) {
+    // ------------------------------------------- fused raw TMA producer
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      const TileRange tr = tile_range<GROUPED>(tiles, total_tiles);
+      uint8_t* raw = smem + NST * S::STAGE_BYTES;
+      for (int t = tr.first; ok && t < tr.end; t += tr.step) {
+        TcProblem P;
+        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, tiles, t, P);
+        const CUtensorMap* ma = &maps[2 * P.map];
+        const CUtensorMap* mb = &maps[2 * P.map + 1];
+        fence_tensormap(ma);
+        fence_tensormap(mb);
+        for (int kb = 0; kb < P.nkb; ++kb, ++it) {
+          const int s = it % RST;
+          const uint32_t ph = (it / RST) & 1;
+          if (!mbar_wait(&raw_empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
+          uint8_t* ra = raw + s * S::RAW_BYTES;
+          const int k0 = (P.kb0 + kb) * kTcKB;
+          mbar_arrive_expect_tx(&raw_full[s], S::RAW_BYTES);
+          if (P.kc_a) tma_load_2d(ra, ma, &raw_full[s], k0, tc.m0);
+          else tma_load_2d(ra, ma, &raw_full[s], tc.m0, k0);
+          if (P.kc_b) tma_load_2d(ra + S::RAW_A, mb, &raw_full[s], k0, tc.n0);
+          else tma_load_2d(ra + S::RAW_A, mb, &raw_full[s], tc.n0, k0);
+        }
+      }
+      if (!ok) {  // let copies still in flight land before the CTA exits
+        for (uint32_t j = (it > uint32_t(RST) ? it - RST : 0); j < it; ++j)
+          mbar_wait(&raw_full[j % RST], (j / RST) & 1, nullptr, 0);
+      }
+    }
+  } else if (warp == 0) {
     // ------------------------------------------------------ TMA producer
     if (lane == 0) {
       if (!GROUPED) {
@@ -238,8 +300,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         tc_fence_after();
         for (int kb = 0; kb < P.nkb; ++kb, ++it) {
-          const int s = it % S::STAGES;
-          const uint32_t ph = (it / S::STAGES) & 1;
+          const int s = it % NST;
+          const uint32_t ph = (it / NST) & 1;
           if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) { ok = false; break; }
           tc_fence_after();
           const uint32_t sa = base + s * S::STAGE_BYTES;
@@ -280,7 +342,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
     }
     __syncwarp();
-  } else {
+  } else if (warp < 2 + kTcEpiWarps) {
     // ------------------------------------------------------ epilogue warps
     constexpr int HALF = BN / 2;  // columns per epilogue warp
     const int ew = warp - 2;
@@ -387,8 +449,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // 256-wide tiles: each 32 x 32 block goes through shared memory 8
         // rows at a time (lanes 8p..8p+7 hold rows 8p..8p+7), so every store
         // instruction still writes one 128-byte row segment
-        float* stage = reinterpret_cast<float*>(smem + S::STAGES * S::STAGE_BYTES + 256) +
-                       ew * 8 * 33;
+        float* stage = reinterpret_cast<float*>(smem + RING + 256) + ew * 8 * 33;
         const int col = tc.n0 + col_off + lane;
 #pragma unroll
         for (int c32 = 0; c32 < HALF / 32; ++c32) {
@@ -420,8 +481,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       if constexpr (S::STAGE_C) {
         // transpose each 32 x 32 block through shared memory: lane = column,
         // one 128-byte row segment per store instruction
-        float* stage = reinterpret_cast<float*>(smem + S::STAGES * S::STAGE_BYTES + 256) +
-                       ew * 32 * 33;
+        float* stage = reinterpret_cast<float*>(smem + RING + 256) + ew * 32 * 33;
         const int col = tc.n0 + col_off + lane;
 #pragma unroll
         for (int c32 = 0; c32 < HALF / 32; ++c32) {
@@ -516,16 +576,17 @@ __device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t 
     out[1] = *reinterpret_cast<const uint32_t*>(&lo);
     return;
   }
-  float rem[2] = {x0, x1};
+  // one paired conversion per piece (the same rounding as two single ones)
+  float2 rem = make_float2(x0, x1);
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
-    const __nv_bfloat16 a = __float2bfloat16_rn(rem[0]), b = __float2bfloat16_rn(rem[1]);
-    rem[0] -= __bfloat162float(a);
-    rem[1] -= __bfloat162float(b);
-    __nv_bfloat162 two;
-    two.x = a;
-    two.y = b;
+    const __nv_bfloat162 two = __float22bfloat162_rn(rem);
     out[p] = *reinterpret_cast<const uint32_t*>(&two);
+    if (p + 1 < NP) {
+      const float2 back = __bfloat1622float2(two);
+      rem.x -= back.x;
+      rem.y -= back.y;
+    }
   }
 }
 
@@ -967,6 +1028,104 @@ __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob
   }
 }
 
+// --------------------------------------------------------- fused converters
+// A fused stage is the kernel's a tile (128 rows) and b tile (BN rows), 32 k
+// deep, in the raw ring as TMA wrote it: a tile whose source has k
+// contiguous is [rows][32] floats in 128-byte rows with the 128-byte swizzle
+// (16-byte unit u of row r at unit u ^ (r & 7)), one whose source has rows
+// contiguous is [32][rows] floats, unswizzled.  Converter thread ct takes 8-k
+// chunks (row, c), k in [8c, 8c + 8): along rows where the tile is [32][rows]
+// (consecutive threads read consecutive words), else four chunks of a row
+// per four threads (each reads two 16-byte units).  It splits each value into
+// three bf16 pieces as the pre-pass does and stores them as 16-byte rows of
+// the three planes at the 64-byte-swizzled position the piece copies would
+// have had (byte offset r * 64 + 16 c, its 16-byte unit index XORed with
+// bits 1-2 of the row), then makes its stores visible to the tensor core
+// (fence.proxy.async) and arrives on the piece stage's full barrier and the
+// raw stage's empty barrier.
+template <int NP, int BN>
+__device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
+                              uint8_t* pieces, uint8_t* raw, uint64_t* full, uint64_t* empty,
+                              uint64_t* raw_full, uint64_t* raw_empty, int ct, int* err) {
+  using S = TcShape<NP, BN, false>;
+  constexpr int CH_A = kTcBM * (kTcKB / 8);
+  constexpr int CH = CH_A + BN * (kTcKB / 8);
+  constexpr int PER = (CH + kTcConvThreads - 1) / kTcConvThreads;
+  static_assert(CH_A % 32 == 0, "a warp's chunks are all of one operand");
+  static_assert(kTcKB == 32, "32-deep stages: 128-byte raw rows, 64-byte piece rows");
+  const int4 range = tiles[blockIdx.x];
+  uint32_t it = 0;
+  for (int t = range.x; t < range.y; ++t) {
+    const int4 rec = tiles[gridDim.x + t];
+    const TcProblem& P = probs[rec.x];
+    const int nkb = P.nkb, kc_a = P.kc_a, kc_b = P.kc_b;
+    for (int kb = 0; kb < nkb; ++kb, ++it) {
+      const int rs = it % kTcRawStages, ps = it % kTcFusedPieceStages;
+      const bool got = mbar_wait(&raw_full[rs], (it / kTcRawStages) & 1, err, kDevTimeoutFull) &&
+                       mbar_wait(&empty[ps], ((it / kTcFusedPieceStages) & 1) ^ 1, err,
+                                 kDevTimeoutEmpty);
+      if (!__all_sync(0xffffffffu, got)) return;
+      const uint8_t* ra = raw + rs * S::RAW_BYTES;
+      uint8_t* pa = pieces + ps * S::STAGE_BYTES;
+      // two chunks at a time, both loaded before either is stored (the
+      // compiler cannot tell the raw and piece rings apart)
+#pragma unroll 1
+      for (int i = 0; i < PER; i += 2) {
+        float v[2][8];
+        int r[2], c[2];
+        bool live[2], is_a[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int ch = ct + kTcConvThreads * (i + u);
+          live[u] = i + u < PER && (CH % kTcConvThreads == 0 || ch < CH);
+          is_a[u] = ch < CH_A;
+          if (!live[u]) continue;
+          const int local = is_a[u] ? ch : ch - CH_A, nrows = is_a[u] ? kTcBM : BN;
+          const uint8_t* src = is_a[u] ? ra : ra + S::RAW_A;
+          if (is_a[u] ? kc_a : kc_b) {  // [rows][32] floats, 128-byte swizzle
+            r[u] = local >> 2;
+            c[u] = local & 3;
+            const uint8_t* row = src + r[u] * 128;
+            const float4 lo = *reinterpret_cast<const float4*>(row + (((2 * c[u]) ^ (r[u] & 7)) << 4));
+            const float4 hi =
+                *reinterpret_cast<const float4*>(row + (((2 * c[u] + 1) ^ (r[u] & 7)) << 4));
+            v[u][0] = lo.x; v[u][1] = lo.y; v[u][2] = lo.z; v[u][3] = lo.w;
+            v[u][4] = hi.x; v[u][5] = hi.y; v[u][6] = hi.z; v[u][7] = hi.w;
+          } else {   // [32][rows] floats
+            r[u] = local % nrows;
+            c[u] = local / nrows;
+            const float* col = reinterpret_cast<const float*>(src) + (8 * c[u]) * nrows + r[u];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[u][e] = col[e * nrows];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (!live[u]) continue;
+          uint32_t packed[NP][4];
+#pragma unroll
+          for (int e = 0; e < 8; e += 2) {
+            uint32_t two[NP];
+            pieces_pair<NP, 0>(v[u][e], v[u][e + 1], 0, two);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
+          }
+          uint8_t* base = is_a[u] ? pa : pa + S::A_BYTES;
+          const int plane = is_a[u] ? S::A_PLANE : S::B_PLANE;
+          const uint32_t off = static_cast<uint32_t>(r[u]) * 64 + ((c[u] ^ ((r[u] >> 1) & 3)) << 4);
+#pragma unroll
+          for (int p = 0; p < NP; ++p)
+            *reinterpret_cast<uint4*>(base + p * plane + off) =
+                make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+        }
+      }
+      fence_proxy_async();
+      mbar_arrive(&full[ps]);
+      mbar_arrive(&raw_empty[rs]);
+    }
+  }
+}
+
 template <int NP, int FMT>
 void launch_split(const float* src, long long sr, long long sk, int rows, int K, int Kp,
                   __nv_bfloat16* dst, cudaStream_t st, const unsigned* fmax = nullptr) {
@@ -987,19 +1146,21 @@ int sm_count() {
   return sms;
 }
 
-template <int NP, int BN, bool GROUPED, bool EPI, bool TF32>
+template <int NP, int BN, bool GROUPED, bool EPI, bool TF32, bool FUSED = false>
 ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const TcProblem& single,
                            const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
                            int total_tiles, int nprod, int chunk_kb, int max_ctas, int fmt,
                            int* dev_err, cudaStream_t st) {
   using S = TcShape<NP, BN, (split_stage_k(NP) > kTcKB)>;
-  auto kern = split_tc_kernel<NP, BN, GROUPED, EPI, TF32>;
+  auto kern = split_tc_kernel<NP, BN, GROUPED, EPI, TF32, FUSED>;
   static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
-  if (!smem_attr_once(kern, S::SMEM, attr_done)) return UGEMM_ERR_CUDA;
+  constexpr size_t kSmem = FUSED ? S::SMEM_FUSED : S::SMEM;
+  static_assert(kSmem <= 232448, "shared memory budget");
+  if (!smem_attr_once(kern, kSmem, attr_done)) return UGEMM_ERR_CUDA;
   const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
-  kern<<<grid, kTcThreads, S::SMEM, st>>>(ta, tb, single, maps, probs, tiles, total_tiles, nprod,
-                                          chunk_kb, fmt, dev_err);
+  kern<<<grid, FUSED ? kTcFusedThreads : kTcThreads, kSmem, st>>>(
+      ta, tb, single, maps, probs, tiles, total_tiles, nprod, chunk_kb, fmt, dev_err);
   prof_end(st, GROUPED ? kProfGrouped : kProfSplitGemm);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }
@@ -1176,6 +1337,15 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                int chunk_kb,
                                int max_ctas, int* dev_err, cudaStream_t st) {
   const bool grouped = probs != nullptr;
+  if (p.fused) {  // grouped launches of three bf16 pieces in 128-wide tiles only
+    if (p.pieces != 3 || p.block_n != 128 || !grouped) return UGEMM_ERR_ARG;
+    return p.epi ? launch_kernel<3, 128, true, true, false, true>(
+                       ta, tb, single, maps, probs, tiles, total_tiles, p.products, chunk_kb,
+                       max_ctas, 0, dev_err, st)
+                 : launch_kernel<3, 128, true, false, false, true>(
+                       ta, tb, single, maps, probs, tiles, total_tiles, p.products, chunk_kb,
+                       max_ctas, 0, dev_err, st);
+  }
   const int fmt = p.f16 ? 1 : 0;
   const bool tf32 = p.pieces == kPiecesTf32;
 #define UGEMM_SPLIT_CASE(NP, BN, GR, EPI, T)                                                     \
@@ -1223,6 +1393,17 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
 }
 
 int split_kp(int K) { return kp_of(K); }
+
+bool fused_encode_map(const float* base, long long ld, int R, int Cc, bool kcontig, int box_rows,
+                      CUtensorMap* map) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld & 3) || R < 1 || Cc < 1) return false;
+  // the stored matrix: R rows of Cc floats; the box is 32 k by box_rows rows
+  // of the kernel operand, k along the columns (kcontig) or along the rows
+  return kcontig ? encode_tmap_2d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, Cc, R, ld * 4ull,
+                                  kTcKB, box_rows, CU_TENSOR_MAP_SWIZZLE_128B)
+                 : encode_tmap_2d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, Cc, R, ld * 4ull,
+                                  box_rows, kTcKB, CU_TENSOR_MAP_SWIZZLE_NONE);
+}
 
 }  // namespace ugemm
 

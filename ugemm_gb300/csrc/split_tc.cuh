@@ -15,6 +15,17 @@ constexpr int kTcBM = 128;       // rows of C per CTA tile (UMMA M)
 constexpr int kTcKB = 32;        // k depth of one pipeline stage (64-byte bf16 rows)
 constexpr int kTcEpiWarps = 8;   // two per TMEM lane quarter
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
+// Fused launches (the operands split inside the GEMM kernel): warp 0's TMA
+// copies bring raw FP32 tiles of the operands into a ring of kTcRawStages
+// stages, and kTcConvWarps more warps after the epilogue warps (six: sixteen
+// warps in all, 128 registers each) convert each
+// into the three bf16 pieces of a piece stage (kTcFusedPieceStages of them),
+// which the MMA issuer reads as it reads pre-split pieces.
+constexpr int kTcConvWarps = 6;
+constexpr int kTcConvThreads = kTcConvWarps * 32;
+constexpr int kTcFusedThreads = kTcThreads + kTcConvThreads;
+constexpr int kTcFusedPieceStages = 2;
+constexpr int kTcRawStages = 3;
 constexpr int kTcRaster = 8;     // tile rows per raster group (L2 reuse)
 
 // FP16x3 form: every row of an operand's K-major piece matrix -- a row of
@@ -92,6 +103,13 @@ struct TcShape {
   static constexpr size_t STAGE_C8_BYTES = STAGE_C8 ? size_t(kTcEpiWarps) * 8 * 33 * 4 : 0;
   static constexpr size_t SMEM =
       1024 + size_t(STAGES) * STAGE_BYTES + 256 + STAGE_C_BYTES + STAGE_C8_BYTES;
+  // fused launches: kTcFusedPieceStages piece stages, then kTcRawStages raw
+  // FP32 stages (the a tile, then the b tile, 32 k deep)
+  static constexpr int RAW_A = kTcBM * kTcKB * 4;
+  static constexpr int RAW_BYTES = RAW_A + BN * kTcKB * 4;
+  static constexpr size_t FUSED_RING =
+      size_t(kTcFusedPieceStages) * STAGE_BYTES + size_t(kTcRawStages) * RAW_BYTES;
+  static constexpr size_t SMEM_FUSED = 1024 + FUSED_RING + 256 + STAGE_C_BYTES + STAGE_C8_BYTES;
   // main + correction accumulators, double-buffered across tiles when they fit
   static constexpr int ACC_BUFS = (4 * BN <= 512) ? 2 : 1;
   static constexpr uint32_t TMEM_COLS = ACC_BUFS * 2 * BN;
@@ -123,6 +141,11 @@ struct TcProblem {
   // Null otherwise.
   const unsigned* fmax_a = nullptr;
   const unsigned* fmax_b = nullptr;
+  // fused launches: whether the raw tile of the kernel's a (b) operand has k
+  // contiguous (the map's box is {32 k, rows}, 128-byte swizzle) or rows
+  // contiguous (box {rows, 32 k}, no swizzle); maps[2 * map] and
+  // maps[2 * map + 1] then describe the FP32 sources
+  int kc_a = 1, kc_b = 1;
 };
 
 // One operand to split in the batched pre-pass.
@@ -199,10 +222,17 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
 // probs/tiles: a grouped launch's problem records and its tile table (from
 // split_tile_table, for a grid of exactly max_ctas CTAs); both null for one
 // GEMM (`single`).
+// p.fused (grouped only): `maps` describe the FP32 operands, not pieces.
 ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const CUtensorMap& tb,
                                const TcProblem& single, const CUtensorMap* maps,
                                const TcProblem* probs, const int4* tiles, int total_tiles,
                                int chunk_kb, int max_ctas, int* dev_err, cudaStream_t st);
+// The TMA map of a fused launch's FP32 operand stored as R rows x Cc columns
+// (leading dimension ld elements): kcontig, the kernel reads k along the
+// columns (box {32, box_rows}, 128-byte swizzle); else rows along them (box
+// {box_rows, 32}).  False if TMA cannot describe it (alignment).
+bool fused_encode_map(const float* base, long long ld, int R, int Cc, bool kcontig, int box_rows,
+                      CUtensorMap* map);
 // Tile table of a grouped launch of `grid` persistent CTAs: grid ranges
 // {first, end, 0, 0} into the records that follow, one {problem, m0, n0, 0}
 // per tile (raster order within a problem), dealt longest first to the

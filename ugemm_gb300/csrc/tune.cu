@@ -59,7 +59,8 @@ uint64_t signature(int count, const ugemm_problem* q, int form) {
 }
 
 // One cache line: the chosen configuration and its time, then every
-// candidate timed as [block_n, chunk_k, max_ctas, split_k, deal, transpose, ms].
+// candidate timed as [block_n, chunk_k, max_ctas, split_k, deal, transpose,
+// fused, ms].
 bool lookup(const std::string& dev, int form, uint64_t sig, ugemm_tile_config* cfg, double* ms) {
   FILE* f = std::fopen(cache_path().c_str(), "r");
   if (!f) return false;
@@ -74,9 +75,9 @@ bool lookup(const std::string& dev, int form, uint64_t sig, ugemm_tile_config* c
     if (std::sscanf(line.data(),
                     "{\"device\": \"%127[^\"]\", \"form\": %d, \"sig\": \"%" SCNx64
                     "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"split_k\": %d, "
-                    "\"deal\": %d, \"transpose\": %d, \"ms\": %lf",
+                    "\"deal\": %d, \"transpose\": %d, \"fused\": %d, \"ms\": %lf",
                     d, &fm, &s, &c.block_n, &c.chunk_k, &c.max_ctas, &c.split_k, &c.deal,
-                    &c.transpose, &t) == 10 &&
+                    &c.transpose, &c.fused, &t) == 11 &&
         dev == d && fm == form && s == sig) {
       *cfg = c;
       if (ms) *ms = t;
@@ -99,13 +100,14 @@ void store(const std::string& dev, int form, uint64_t sig, const ugemm_tile_conf
   std::fprintf(f,
                "{\"device\": \"%s\", \"form\": %d, \"sig\": \"%016" PRIx64
                "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"split_k\": %d, "
-               "\"deal\": %d, \"transpose\": %d, \"ms\": %.6f, \"candidates\": [",
+               "\"deal\": %d, \"transpose\": %d, \"fused\": %d, \"ms\": %.6f, "
+               "\"candidates\": [",
                dev.c_str(), form, sig, c.block_n, c.chunk_k, c.max_ctas, c.split_k, c.deal,
-               c.transpose, ms);
+               c.transpose, c.fused, ms);
   for (size_t i = 0; i < all.size(); ++i) {
     const ugemm_tile_config& x = all[i].c;
-    std::fprintf(f, "%s[%d, %d, %d, %d, %d, %d, %.6f]", i ? ", " : "", x.block_n, x.chunk_k,
-                 x.max_ctas, x.split_k, x.deal, x.transpose, all[i].ms);
+    std::fprintf(f, "%s[%d, %d, %d, %d, %d, %d, %d, %.6f]", i ? ", " : "", x.block_n,
+                 x.chunk_k, x.max_ctas, x.split_k, x.deal, x.transpose, x.fused, all[i].ms);
   }
   std::fprintf(f, "]}\n");
   std::fclose(f);
@@ -183,11 +185,14 @@ UGEMM_API int ugemm_tune_grouped(int count, const ugemm_problem* problems, int p
   };
   // 1. tile shape
   if (form == UGEMM_PREC_SIMT) {
-    for (int bn : {64, 128}) consider(ugemm_tile_config{bn, 0, 0, 0, 0, 0});
+    for (int bn : {64, 128}) consider(ugemm_tile_config{bn, 0, 0, 0, 0, 0, 0});
   } else {
     // chunk_k <= 256 keeps the split form at least as accurate as FP32 SIMT
     for (int bn : {128, 256})
-      for (int ck : {128, 256}) consider(ugemm_tile_config{bn, ck, 0, 0, 0, 0});
+      for (int ck : {128, 256}) consider(ugemm_tile_config{bn, ck, 0, 0, 0, 0, 0});
+    // three bf16 pieces: the operands split inside the GEMM kernel (128-wide)
+    if (form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9)
+      for (int ck : {128, 256}) consider(ugemm_tile_config{128, ck, 0, 0, 0, 0, 1});
   }
   // 2. schedule, one knob at a time from the best so far
   if (cur_t < 1e30) {
