@@ -133,19 +133,27 @@ def cpu_sample(steps: int = 1):
 
 def grouped_forms(ug, torch, stream, steps):
     """TFLOPS of the 256-problem grouped SGEMM (config 4) in both forms, each
-    a tuned plan replayed as a CUDA graph, timed with CUDA events."""
+    a tuned plan replayed as a CUDA graph, timed with CUDA events.  Operand
+    rows are padded to a multiple of 4 floats (16 bytes), as a caller that
+    wants the fused launches (operands copied by TMA, which needs 16-byte
+    strides) allocates them; the tuner may still pick a pre-pass launch."""
     from ugemm_gb300 import workloads
     shapes = workloads.grouped_shapes()
     gen = torch.Generator(device="cuda").manual_seed(SEED + 7)
     specs, refs = [], []
+
+    def padded(rows, cols):
+        return (torch.rand((rows, -(-cols // 4) * 4), device="cuda", generator=gen) * 2 - 1)[:, :cols]
+
     for (ta, tb, M, N, K) in shapes:
-        A = torch.rand((M, K) if ta == "N" else (K, M), device="cuda", generator=gen) * 2 - 1
-        B = torch.rand((K, N) if tb == "N" else (N, K), device="cuda", generator=gen) * 2 - 1
+        A = padded(M, K) if ta == "N" else padded(K, M)
+        B = padded(K, N) if tb == "N" else padded(N, K)
         C = torch.zeros((M, N), device="cuda")
         specs.append(dict(ta=ta, tb=tb, M=M, N=N, K=K, alpha=1.0, beta=0.0, A=A, lda=A.stride(0),
                           B=B, ldb=B.stride(0), C=C, ldc=N))
         refs.append(ug.ref64(ta, tb, A, B))
-    out = {"problems": len(shapes), "flops": sum(2.0 * m * n * k for _, _, m, n, k in shapes)}
+    out = {"problems": len(shapes), "flops": sum(2.0 * m * n * k for _, _, m, n, k in shapes),
+           "operand_rows": "padded to 16 bytes"}
     for prec in ("bf16x6", "fp16x3", "simt"):
         cfg, _ = ug.tune_grouped(specs, precision=prec)
         plan = ug.GroupedPlan(specs, precision=prec, config=cfg, graph=True)
@@ -163,9 +171,10 @@ def grouped_forms(ug, torch, stream, steps):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
+        launches = 1 if plan.config.get("fused") else (3 if prec == "fp16x3" else 2)
         out[prec] = {"tflops": round(out["flops"] / (ms * 1e-3) / 1e12, 3), "ms": round(ms, 4),
                      "max_normwise_err_fp64": err, "config": plan.config,
-                     "launches_per_run": 3 if prec == "fp16x3" else 2}
+                     "launches_per_run": launches}
         plan.close()
     best = max(("bf16x6", "fp16x3"), key=lambda p: out[p]["tflops"])
     out["split_over_simt"] = round(out[best]["tflops"] / out["simt"]["tflops"], 3)
@@ -274,15 +283,23 @@ def profile_case(args):
         for _ in range(reps):
             ug.sgemm_dev("N", "N", n, n, n, 1.0, A, n, B, n, 0.0, C, n, precision=prec)
     else:
+        # the 256-problem group, operand rows padded to 16 bytes as in the
+        # benchmark; grouped_fused: the fused launch (128-wide tiles)
+        def padded(rows, cols):
+            return (torch.rand((rows, -(-cols // 4) * 4), device="cuda") * 2 - 1)[:, :cols]
+
         specs = []
         for (ta, tb, M, N, K) in workloads.grouped_shapes():
-            A = torch.rand((M, K) if ta == "N" else (K, M), device="cuda") * 2 - 1
-            B = torch.rand((K, N) if tb == "N" else (N, K), device="cuda") * 2 - 1
+            A = padded(M, K) if ta == "N" else padded(K, M)
+            B = padded(K, N) if tb == "N" else padded(N, K)
             C = torch.zeros((M, N), device="cuda")
             specs.append(dict(ta=ta, tb=tb, M=M, N=N, K=K, alpha=1.0, beta=0.0, A=A,
                               lda=A.stride(0), B=B, ldb=B.stride(0), C=C, ldc=N))
-        prec = "bf16x6" if args.profile_case == "grouped_split" else "simt"
-        plan = ug.GroupedPlan(specs, precision=prec)
+        prec = "simt" if args.profile_case == "grouped_simt" else "bf16x6"
+        cfg = dict(block_n=128, chunk_k=256, fused=1) if args.profile_case == "grouped_fused" else None
+        plan = ug.GroupedPlan(specs, precision=prec, config=cfg)
+        if cfg and not plan.config["fused"]:
+            raise RuntimeError("grouped_fused: the plan could not take the fused launch")
         for _ in range(reps):
             plan.run()
         plan.check()
@@ -374,8 +391,8 @@ def main():
     ap.add_argument("--size", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--profile-case", default=None,
-                    choices=["split", "split_fp16", "simt", "grouped_split", "grouped_simt",
-                             "conv_split"],
+                    choices=["split", "split_fp16", "simt", "grouped_split", "grouped_fused",
+                             "grouped_simt", "conv_split"],
                     help="run only this case --steps times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.impl == "reference":

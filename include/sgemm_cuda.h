@@ -237,8 +237,8 @@ typedef struct {
   int transpose; /* split form: 0 = compute C^T = op(B)^T op(A)^T where that wastes less of
                     the 128-row tiles, 1 = never */
   int fused;     /* BF16X6 / BF16X9: 1 = the GEMM kernel copies the FP32 operands with TMA
-                    and splits them itself (no pre-pass, no pieces in memory; 128-wide
-                    tiles), 0 = a pre-pass launch writes the pieces first.  Taken only when
+                    and splits them itself (no pre-pass, no pieces in memory), 0 = a
+                    pre-pass launch writes the pieces first.  Taken only when
                     every problem has k > 0, unit-stride operands and 16-byte aligned bases
                     and leading dimensions (implicit im2col operands take the pre-pass);
                     the plan's config reports whether it was */

@@ -1,9 +1,11 @@
 """Fused grouped launches: the GEMM kernel copies the FP32 operand tiles
-into shared memory itself and converter warps split them into the three
+into shared memory itself and converter threads split them into the three
 bf16 pieces in the layout the piece copies would have had, instead of a
-pre-pass writing the pieces to memory first.  The pieces, the tile schedule
-and the MMA order are the pre-pass launch's, so with the same tile shape the
-results must be the same bits; they are also checked against FP64."""
+pre-pass writing the pieces to memory first.  The pieces, the tile schedule,
+the MMA order and the order in which chunk sums are added are the pre-pass
+launch's, so with the same tile shape (128 wide: separate converter warps;
+256 wide: the epilogue warps convert and keep chunk sums in global memory)
+the results must be the same bits; they are also checked against FP64."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -22,11 +24,11 @@ def gpu():
     ug.load()
 
 
-def run_plan(specs, prec, fused, chunk_k=256, expect=None):
+def run_plan(specs, prec, fused, chunk_k=256, expect=None, block_n=128):
     for s in specs:
         s["C"].copy_(s["C0"])
     plan = ug.GroupedPlan(specs, precision=prec,
-                          config={"block_n": 128, "chunk_k": chunk_k, "fused": int(fused)})
+                          config={"block_n": block_n, "chunk_k": chunk_k, "fused": int(fused)})
     assert plan.config["fused"] == int(fused if expect is None else expect)
     plan.run()
     plan.check()
@@ -40,21 +42,23 @@ def with_c0(specs):
     return specs
 
 
+@pytest.mark.parametrize("block_n", [128, 256])
 @pytest.mark.parametrize("prec", ["bf16x6", "bf16x9"])
-def test_fused_config4_group_is_bit_identical(prec):
+def test_fused_config4_group_is_bit_identical(prec, block_n):
     """The 256-problem group (M, N, K log-uniform in [32, 1024], NN/NT/TN),
     leading dimensions rounded up to 16 bytes."""
     specs, refs = make_group(workloads.grouped_shapes(), seed=2, align=4)
     with_c0(specs)
-    pre = run_plan(specs, prec, fused=False)
-    fus = run_plan(specs, prec, fused=True)
+    pre = run_plan(specs, prec, fused=False, block_n=block_n)
+    fus = run_plan(specs, prec, fused=True, block_n=block_n)
     for a, b in zip(pre, fus):
         assert torch.equal(a, b)
     assert worst_error(specs, refs) < 2e-6
 
 
+@pytest.mark.parametrize("block_n", [128, 256])
 @pytest.mark.parametrize("chunk_k", [64, 256])
-def test_fused_split_k_epilogue_transposes(chunk_k):
+def test_fused_split_k_epilogue_transposes(chunk_k, block_n):
     """Deep-k problems cut into split-K slices, a fused bias + LeakyReLU
     epilogue, padded leading dimensions, every transpose pair, wide problems
     computed transposed, ragged edges in every dimension."""
@@ -67,8 +71,8 @@ def test_fused_split_k_epilogue_transposes(chunk_k):
         s["bias"] = torch.rand((s["M"],), device="cuda", generator=g)
         s["act"], s["slope"] = 1, 0.1
     with_c0(specs)
-    pre = run_plan(specs, "bf16x6", fused=False, chunk_k=chunk_k)
-    fus = run_plan(specs, "bf16x6", fused=True, chunk_k=chunk_k)
+    pre = run_plan(specs, "bf16x6", fused=False, chunk_k=chunk_k, block_n=block_n)
+    fus = run_plan(specs, "bf16x6", fused=True, chunk_k=chunk_k, block_n=block_n)
     for a, b in zip(pre, fus):
         assert torch.equal(a, b)
     # the problems without an epilogue against FP64

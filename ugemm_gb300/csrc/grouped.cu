@@ -74,6 +74,7 @@ struct ugemm_grouped_plan_s {
   int nsub = 0;                   // kernel problems (split-K slices count one each)
   const void* reduce = nullptr;   // split-K reduce jobs
   const int4* tiles = nullptr;    // split form: per-CTA ranges, then one record per tile
+  float* chunk_sums = nullptr;    // fused 256-wide launches: kTcFusedSumBytes per CTA
   unsigned* fmax = nullptr;       // FP16x3: the largest magnitude of every operand row
   int nfmax = 0;                  // words at fmax
   int grid = 0;                   // split form: persistent CTAs the tile table is dealt to
@@ -117,6 +118,7 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   TcProblem single{};
+  single.chunk_sums = p->chunk_sums;
   s = split_gemm_launch(p->split, dummy, dummy, single, p->maps,
                         static_cast<const TcProblem*>(p->probs), p->tiles, p->gemm_tiles,
                         split_chunk_stages(p->split.pieces, std::max(1, p->cfg.chunk_k / kTcKB)),
@@ -128,13 +130,13 @@ ugemm_status launch_plan(ugemm_grouped_plan_s* p, cudaStream_t st) {
 // or of op(B)^T, by k) as a 2-D tensor map: k contiguous (row stride sr) or
 // rows contiguous (k stride sk).  *kc says which.
 bool fused_operand_map(const float* base, long long sr, long long sk, int rows, int K,
-                       int box_rows, CUtensorMap* map, int* kc) {
+                       int box_rows, int box_k, CUtensorMap* map, int* kc) {
   if (sk == 1) {
     *kc = 1;
-    return fused_encode_map(base, sr, rows, K, true, box_rows, map);
+    return fused_encode_map(base, sr, rows, K, true, box_rows, box_k, map);
   }
   *kc = 0;
-  return sr == 1 && fused_encode_map(base, sk, K, rows, false, box_rows, map);
+  return sr == 1 && fused_encode_map(base, sk, K, rows, false, box_rows, box_k, map);
 }
 
 // A fused launch copies the FP32 operands with TMA: each needs a unit
@@ -256,12 +258,11 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
     }
   }
   if (form != UGEMM_PREC_SIMT) {
-    // fused launches split three bf16 pieces inside the GEMM kernel, with
-    // 128-wide tiles; other forms ignore the knob
+    // fused launches split three bf16 pieces inside the GEMM kernel (128-
+    // or 256-wide tiles); other forms ignore the knob
     const bool can_fuse = split_plan_for(form, g[0]).pieces == 3 &&
                           std::all_of(g.begin(), g.end(), fusable);
-    if (p->cfg.fused && can_fuse) p->cfg.block_n = 128;
-    else p->cfg.fused = 0;
+    if (!(p->cfg.fused && can_fuse)) p->cfg.fused = 0;
     if (p->cfg.block_n != 128 && p->cfg.block_n != 256) p->cfg.block_n = 256;
     if (p->cfg.chunk_k < kTcKB) p->cfg.chunk_k = split_default_chunk_kb(1 << 30) * kTcKB;
   } else {
@@ -361,6 +362,10 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
   }
   const size_t part_base = scratch;
   scratch += part_bytes;
+  // fused 256-wide launches: the chunk sums of every persistent CTA
+  const size_t sums_base = scratch;
+  if (!simt && p->split.fused && bn == 256)
+    scratch += size_t(std::max(1, p->cfg.max_ctas > 0 ? p->cfg.max_ctas : sms)) * kTcFusedSumBytes;
   cudaError_t e = cudaMalloc(&p->scratch, std::max<size_t>(scratch, 256));
   // zeroed once: a K == 0 problem's slot is read as one zero k tile
   if (e == cudaSuccess) e = cudaMemset(p->scratch, 0, std::max<size_t>(scratch, 256));
@@ -371,6 +376,7 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
     return plan_fail(UGEMM_ERR_ALLOC, "cudaMalloc for the grouped plan failed");
   }
   uint8_t* base = static_cast<uint8_t*>(p->scratch);
+  if (!simt && p->split.fused && bn == 256) p->chunk_sums = reinterpret_cast<float*>(base + sums_base);
 
   // pre-pass jobs: one per operand of every problem
   std::vector<SplitJob> sjobs;
@@ -455,11 +461,14 @@ ugemm_status grouped_plan_build(const Gemm* gs, int count, int form,
         // when the problem is computed transposed
         long long a_sr, a_sk, b_sr, b_sk;
         split_operand_strides(x, &a_sr, &a_sk, &b_sr, &b_sk);
-        ok = o.swap ? fused_operand_map(x.B, b_sr, b_sk, x.N, x.K, kTcBM, &maps[2 * i], &tp.kc_a) &&
-                          fused_operand_map(x.A, a_sr, a_sk, x.M, x.K, bn, &maps[2 * i + 1],
+        const int bk = fused_raw_k(bn);
+        ok = o.swap ? fused_operand_map(x.B, b_sr, b_sk, x.N, x.K, kTcBM, bk, &maps[2 * i],
+                                        &tp.kc_a) &&
+                          fused_operand_map(x.A, a_sr, a_sk, x.M, x.K, bn, bk, &maps[2 * i + 1],
                                             &tp.kc_b)
-                    : fused_operand_map(x.A, a_sr, a_sk, x.M, x.K, kTcBM, &maps[2 * i], &tp.kc_a) &&
-                          fused_operand_map(x.B, b_sr, b_sk, x.N, x.K, bn, &maps[2 * i + 1],
+                    : fused_operand_map(x.A, a_sr, a_sk, x.M, x.K, kTcBM, bk, &maps[2 * i],
+                                        &tp.kc_a) &&
+                          fused_operand_map(x.B, b_sr, b_sk, x.N, x.K, bn, bk, &maps[2 * i + 1],
                                             &tp.kc_b);
       } else {
         const void* da = base + a_off[u.j];

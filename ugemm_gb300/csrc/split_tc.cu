@@ -115,11 +115,195 @@ __device__ __forceinline__ TileCoord tile_coord(const TcProblem& single, const T
   return tc;
 }
 
+// The end of a tile's epilogue once acc holds its sums (this warp's HALF
+// columns of its lane quarter's 32 rows): the FP16x3 scales, alpha/beta (C is
+// read only when beta != 0), the bias / activation (EPI instantiations only)
+// and the stores.  stage_base: the shared-memory staging area after the ring.
+template <int NP, int BN, bool GROUPED, bool EPI>
+__device__ __forceinline__ void epi_store(const TcProblem& P, const TileCoord& tc,
+                                          float (&acc)[BN / 2], int warp, int lane,
+                                          float* stage_base) {
+  using S = TcShape<NP, BN, (split_stage_k(NP) > kTcKB)>;
+  constexpr int HALF = BN / 2;
+  const int ew = warp - 2;
+  const int q = warp & 3;
+  const int col_off = (ew >> 2) * HALF;
+  const int n_live = GROUPED ? P.N - tc.n0 - col_off : HALF;
+  (void)n_live;
+  if constexpr (NP == 2) {  // FP16x3: undo the rows' and columns' power-of-two scales
+    if (P.fmax_a != nullptr) {
+      // this lane's row; lane l fetches the scales of columns l, l + 32, ...
+      // of the warp's half and hands them to the other lanes by shuffle
+      const int row = tc.m0 + q * 32 + lane;
+      const int ea = row < P.M ? f16_scale_exp(P.fmax_a[row]) : 0;
+      int eb[HALF / 32];
+#pragma unroll
+      for (int c32 = 0; c32 < HALF / 32; ++c32) {
+        const int col = tc.n0 + col_off + c32 * 32 + lane;
+        eb[c32] = col < P.N ? f16_scale_exp(P.fmax_b[col]) : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < HALF; ++j)
+        acc[j] = scale_pow2(acc[j], -(ea + __shfl_sync(0xffffffffu, eb[j / 32], j % 32)));
+    }
+  }
+  // alpha/beta epilogue (C not read when beta == 0).  The bias /
+  // activation exists only in the EPI instantiation, so the plain kernel's
+  // epilogue carries no code for it.
+  const bool has_epi = EPI && (P.epi.bias != nullptr || P.epi.act != 0);
+  if (GROUPED && P.swap) {
+    // transposed problem: this lane's kernel row is a C column, so for a
+    // fixed register the warp writes 32 consecutive floats of one C row
+    const int r = tc.m0 + q * 32 + lane;
+    if (r < P.M) {
+#pragma unroll
+      for (int j = 0; j < HALF; ++j) {
+        const int c = tc.n0 + col_off + j;
+        if (c < P.N) {
+          float* cp = P.C + static_cast<size_t>(c) * P.ldc + r;
+          float v = P.alpha * acc[j];
+          if (P.beta != 0.f) v += P.beta * *cp;
+          if (has_epi) v = epilogue_apply(v, P.epi, c);
+          *cp = v;
+        }
+      }
+    }
+    return;
+  }
+  if constexpr (GROUPED && S::STAGE_C8) {
+    // 256-wide tiles: each 32 x 32 block goes through shared memory 8
+    // rows at a time (lanes 8p..8p+7 hold rows 8p..8p+7), so every store
+    // instruction still writes one 128-byte row segment
+    float* stage = stage_base + ew * 8 * 33;
+    const int col = tc.n0 + col_off + lane;
+#pragma unroll
+    for (int c32 = 0; c32 < HALF / 32; ++c32) {
+      if (c32 * 32 >= n_live) break;
+      const int cc = col + c32 * 32;
+#pragma unroll
+      for (int pass = 0; pass < 4; ++pass) {
+        if ((lane >> 3) == pass) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) stage[(lane & 7) * 33 + j] = acc[c32 * 32 + j];
+        }
+        __syncwarp();
+        if (cc < P.N) {
+          for (int rr = 0; rr < 8; ++rr) {
+            const int row = tc.m0 + q * 32 + pass * 8 + rr;
+            if (row >= P.M) break;
+            float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
+            float v = P.alpha * stage[rr * 33 + lane];
+            if (P.beta != 0.f) v += P.beta * *cp;
+            if (has_epi) v = epilogue_apply(v, P.epi, row);
+            *cp = v;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    return;
+  }
+  if constexpr (S::STAGE_C) {
+    // transpose each 32 x 32 block through shared memory: lane = column,
+    // one 128-byte row segment per store instruction
+    float* stage = stage_base + ew * 32 * 33;
+    const int col = tc.n0 + col_off + lane;
+#pragma unroll
+    for (int c32 = 0; c32 < HALF / 32; ++c32) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = acc[c32 * 32 + j];
+      __syncwarp();
+      const int cc = col + c32 * 32;
+      if (cc < P.N) {
+        if (has_epi) {
+          for (int rr = 0; rr < 32; ++rr) {
+            const int row = tc.m0 + q * 32 + rr;
+            if (row >= P.M) break;
+            float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
+            float v = P.alpha * stage[rr * 33 + lane];
+            if (P.beta != 0.f) v += P.beta * *cp;
+            *cp = epilogue_apply(v, P.epi, row);
+          }
+        } else {
+          for (int rr = 0; rr < 32; ++rr) {
+            const int row = tc.m0 + q * 32 + rr;
+            if (row >= P.M) break;
+            float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
+            float v = P.alpha * stage[rr * 33 + lane];
+            if (P.beta != 0.f) v += P.beta * *cp;
+            *cp = v;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    return;
+  }
+  const int row = tc.m0 + q * 32 + lane;
+  if (row < P.M) {
+    float* crow = P.C + static_cast<size_t>(row) * P.ldc;
+    const int col0 = tc.n0 + col_off;
+    const bool vec = ((P.ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(P.C) & 15) == 0);
+    if (has_epi) {
+#pragma unroll
+      for (int j = 0; j < HALF; ++j)
+        if (col0 + j < P.N) {
+          float v = P.alpha * acc[j];
+          if (P.beta != 0.f) v += P.beta * crow[col0 + j];
+          crow[col0 + j] = epilogue_apply(v, P.epi, row);
+        }
+    } else if (vec && col0 + HALF <= P.N) {
+#pragma unroll
+      for (int j = 0; j < HALF; j += 4) {
+        float4 v = make_float4(P.alpha * acc[j], P.alpha * acc[j + 1], P.alpha * acc[j + 2],
+                               P.alpha * acc[j + 3]);
+        if (P.beta != 0.f) {
+          const float4 o = *reinterpret_cast<const float4*>(crow + col0 + j);
+          v.x += P.beta * o.x; v.y += P.beta * o.y; v.z += P.beta * o.z; v.w += P.beta * o.w;
+        }
+        *reinterpret_cast<float4*>(crow + col0 + j) = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < HALF; ++j)
+        if (col0 + j < P.N) {
+          float v = P.alpha * acc[j];
+          if (P.beta != 0.f) v += P.beta * crow[col0 + j];
+          crow[col0 + j] = v;
+        }
+    }
+  }
+}
+
+// Adds the accumulator columns this warp owns (TMEM address t: its lane
+// quarter, first column) to acc, 32 columns at a time; grouped launches skip
+// the slices past the tile's n_live result columns.
+template <int HALF, bool GROUPED>
+__device__ __forceinline__ void acc_add_tmem(uint32_t t, float (&acc)[HALF], int n_live) {
+#pragma unroll
+  for (int c32 = 0; c32 < HALF / 32; ++c32) {
+    if (GROUPED && c32 * 32 >= n_live) break;
+    uint32_t r[32];
+    tmem_ld_32x32b_x32(t + c32 * 32, r);
+    tmem_ld_wait();
+#pragma unroll
+    for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
+  }
+}
+
 // The converter warps of a fused launch (defined with the split helpers).
 template <int NP, int BN>
 __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                               uint8_t* pieces, uint8_t* raw, uint64_t* full, uint64_t* empty,
                               uint64_t* raw_full, uint64_t* raw_empty, int ct, int* err);
+// The epilogue warps of a 256-wide fused launch, which also convert.
+template <int NP, int BN, bool EPI>
+__device__ void fused_dual(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
+                           float* chunk_sums, uint8_t* smem, uint32_t tmem, uint64_t* full,
+                           uint64_t* empty, uint64_t* raw_full, uint64_t* raw_empty,
+                           uint64_t* main_full, uint64_t* main_empty, uint64_t* tile_full,
+                           uint64_t* tmem_empty, uint64_t* stage_free, int chunk_kb, int warp,
+                           int lane, int* err);
 
 // TF32: the TF32x3 form's instantiation (two planes of 32-deep tf32
 // stages, tcgen05 kind::tf32), a template parameter so that the 16-bit
@@ -131,7 +315,7 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
 // rows, 64-byte swizzle), so the MMA issuer and the epilogue run unchanged
 // and the results are the same bits.
 template <int NP, int BN, bool GROUPED, bool EPI, bool TF32 = false, bool FUSED = false>
-__global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
+__global__ void __launch_bounds__(FUSED ? fused_threads(BN) : kTcThreads, 1)
     split_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ TcProblem single, const CUtensorMap* __restrict__ maps,
                     const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
@@ -142,6 +326,8 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
   // two-piece 16-bit shape
   static_assert(!TF32 || NP == 2, "TF32 pieces come in two planes");
   static_assert(!FUSED || (NP == 3 && GROUPED && !TF32), "fused: grouped bf16x3-piece launches");
+  // 256-wide fused tiles: the epilogue warps are the converters
+  constexpr bool DUAL = FUSED && BN == 256;
   constexpr bool WIDE = split_stage_k(NP) > kTcKB;
   using S = TcShape<NP, BN, WIDE>;
   constexpr int KB = S::KB;
@@ -164,19 +350,21 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
   uint64_t* main_empty = main_full + NB;     // the epilogue drained it
   uint64_t* tile_full = main_empty + NB;     // all MMAs of a tile are complete
   uint64_t* tmem_empty = tile_full + NB;     // the epilogue read both accumulators
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tmem_empty + NB);
+  uint64_t* stage_free = tmem_empty + NB;    // 256-wide fused: a tile's final epilogue is done
+                                             // with the piece stage it parks sums in
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(stage_free + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; ++s) {
       // a fused piece stage is written by the converter threads, each of
       // which arrives once its stores are visible to the tensor core
-      mbar_init(&full[s], FUSED ? kTcConvThreads : 1);
+      mbar_init(&full[s], FUSED ? fused_conv_threads(BN) : 1);
       mbar_init(&empty[s], 1);
     }
     for (int s = 0; s < RST; ++s) {
       mbar_init(&raw_full[s], 1);
-      mbar_init(&raw_empty[s], kTcConvThreads);
+      mbar_init(&raw_empty[s], fused_conv_threads(BN));
     }
     for (int b = 0; b < NB; ++b) {
       mbar_init(&main_full[b], 1);
@@ -184,6 +372,7 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
       mbar_init(&tile_full[b], 1);
       mbar_init(&tmem_empty[b], kTcEpiWarps);
     }
+    mbar_init(stage_free, kTcEpiWarps);
     fence_barrier_init();
   }
   if (warp == 1) {
@@ -195,9 +384,9 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (FUSED && warp >= 2 + kTcEpiWarps) {
+  if (FUSED && !DUAL && warp >= 2 + kTcEpiWarps) {
     // ------------------------------------------------- fused converters
-    if constexpr (FUSED)
+    if constexpr (FUSED && !DUAL)
       fused_convert<NP, BN>(probs, tiles, smem, smem + NST * S::STAGE_BYTES, full, empty,
                             raw_full, raw_empty, (warp - 2 - kTcEpiWarps) * 32 + lane, err);
   } else if (FUSED && warp == 0) {
@@ -214,12 +403,13 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
         const CUtensorMap* mb = &maps[2 * P.map + 1];
         fence_tensormap(ma);
         fence_tensormap(mb);
-        for (int kb = 0; kb < P.nkb; ++kb, ++it) {
+        // each piece stage from kTcKB / RAW_K raw stages
+        for (int kr = 0; ok && kr < P.nkb * (kTcKB / S::RAW_K); ++kr, ++it) {
           const int s = it % RST;
           const uint32_t ph = (it / RST) & 1;
           if (!mbar_wait(&raw_empty[s], ph ^ 1, err, kDevTimeoutEmpty)) { ok = false; break; }
           uint8_t* ra = raw + s * S::RAW_BYTES;
-          const int k0 = (P.kb0 + kb) * kTcKB;
+          const int k0 = P.kb0 * kTcKB + kr * S::RAW_K;
           mbar_arrive_expect_tx(&raw_full[s], S::RAW_BYTES);
           if (P.kc_a) tma_load_2d(ra, ma, &raw_full[s], k0, tc.m0);
           else tma_load_2d(ra, ma, &raw_full[s], tc.m0, k0);
@@ -342,6 +532,12 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
       }
     }
     __syncwarp();
+  } else if (DUAL) {
+    // ---------------------------------- epilogue warps that also convert
+    if constexpr (DUAL)
+      fused_dual<NP, BN, EPI>(probs, tiles, single.chunk_sums, smem, tmem, full, empty,
+                              raw_full, raw_empty, main_full, main_empty, tile_full, tmem_empty,
+                              stage_free, chunk_kb, warp, lane, err);
   } else if (warp < 2 + kTcEpiWarps) {
     // ------------------------------------------------------ epilogue warps
     constexpr int HALF = BN / 2;  // columns per epilogue warp
@@ -372,15 +568,7 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
         }
         ++nbound[buf];
         tc_fence_after();
-#pragma unroll
-        for (int c32 = 0; c32 < HALF / 32; ++c32) {
-          if (GROUPED && c32 * 32 >= n_live) break;
-          uint32_t r[32];
-          tmem_ld_32x32b_x32(t_buf + c32 * 32, r);
-          tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
-        }
+        acc_add_tmem<HALF, GROUPED>(t_buf, acc, n_live);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&main_empty[buf]);
@@ -390,164 +578,13 @@ __global__ void __launch_bounds__(FUSED ? kTcFusedThreads : kTcThreads, 1)
         break;
       tc_fence_after();
       // last main chunk, then the corrections (one 32-column slice live at a time)
-#pragma unroll
-      for (int part = 0; part < 2; ++part) {
-#pragma unroll
-        for (int c32 = 0; c32 < HALF / 32; ++c32) {
-          if (GROUPED && c32 * 32 >= n_live) break;
-          uint32_t r[32];
-          tmem_ld_32x32b_x32(t_buf + part * BN + c32 * 32, r);
-          tmem_ld_wait();
-#pragma unroll
-          for (int j = 0; j < 32; ++j) acc[c32 * 32 + j] += __uint_as_float(r[j]);
-        }
-      }
+      acc_add_tmem<HALF, GROUPED>(t_buf, acc, n_live);
+      acc_add_tmem<HALF, GROUPED>(t_buf + BN, acc, n_live);
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmem_empty[buf]);
-      if constexpr (NP == 2) {  // FP16x3: undo the rows' and columns' power-of-two scales
-        if (P.fmax_a != nullptr) {
-          // this lane's row; lane l fetches the scales of columns l, l + 32, ...
-          // of the warp's half and hands them to the other lanes by shuffle
-          const int row = tc.m0 + q * 32 + lane;
-          const int ea = row < P.M ? f16_scale_exp(P.fmax_a[row]) : 0;
-          int eb[HALF / 32];
-#pragma unroll
-          for (int c32 = 0; c32 < HALF / 32; ++c32) {
-            const int col = tc.n0 + col_off + c32 * 32 + lane;
-            eb[c32] = col < P.N ? f16_scale_exp(P.fmax_b[col]) : 0;
-          }
-#pragma unroll
-          for (int j = 0; j < HALF; ++j)
-            acc[j] = scale_pow2(acc[j], -(ea + __shfl_sync(0xffffffffu, eb[j / 32], j % 32)));
-        }
-      }
-      // alpha/beta epilogue (C not read when beta == 0).  The bias /
-      // activation exists only in the EPI instantiation, so the plain kernel's
-      // epilogue carries no code for it.
-      const bool has_epi = EPI && (P.epi.bias != nullptr || P.epi.act != 0);
-      if (GROUPED && P.swap) {
-        // transposed problem: this lane's kernel row is a C column, so for a
-        // fixed register the warp writes 32 consecutive floats of one C row
-        const int r = tc.m0 + q * 32 + lane;
-        if (r < P.M) {
-#pragma unroll
-          for (int j = 0; j < HALF; ++j) {
-            const int c = tc.n0 + col_off + j;
-            if (c < P.N) {
-              float* cp = P.C + static_cast<size_t>(c) * P.ldc + r;
-              float v = P.alpha * acc[j];
-              if (P.beta != 0.f) v += P.beta * *cp;
-              if (has_epi) v = epilogue_apply(v, P.epi, c);
-              *cp = v;
-            }
-          }
-        }
-        continue;
-      }
-      if constexpr (GROUPED && S::STAGE_C8) {
-        // 256-wide tiles: each 32 x 32 block goes through shared memory 8
-        // rows at a time (lanes 8p..8p+7 hold rows 8p..8p+7), so every store
-        // instruction still writes one 128-byte row segment
-        float* stage = reinterpret_cast<float*>(smem + RING + 256) + ew * 8 * 33;
-        const int col = tc.n0 + col_off + lane;
-#pragma unroll
-        for (int c32 = 0; c32 < HALF / 32; ++c32) {
-          if (c32 * 32 >= n_live) break;
-          const int cc = col + c32 * 32;
-#pragma unroll
-          for (int pass = 0; pass < 4; ++pass) {
-            if ((lane >> 3) == pass) {
-#pragma unroll
-              for (int j = 0; j < 32; ++j) stage[(lane & 7) * 33 + j] = acc[c32 * 32 + j];
-            }
-            __syncwarp();
-            if (cc < P.N) {
-              for (int rr = 0; rr < 8; ++rr) {
-                const int row = tc.m0 + q * 32 + pass * 8 + rr;
-                if (row >= P.M) break;
-                float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
-                float v = P.alpha * stage[rr * 33 + lane];
-                if (P.beta != 0.f) v += P.beta * *cp;
-                if (has_epi) v = epilogue_apply(v, P.epi, row);
-                *cp = v;
-              }
-            }
-            __syncwarp();
-          }
-        }
-        continue;
-      }
-      if constexpr (S::STAGE_C) {
-        // transpose each 32 x 32 block through shared memory: lane = column,
-        // one 128-byte row segment per store instruction
-        float* stage = reinterpret_cast<float*>(smem + RING + 256) + ew * 32 * 33;
-        const int col = tc.n0 + col_off + lane;
-#pragma unroll
-        for (int c32 = 0; c32 < HALF / 32; ++c32) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) stage[lane * 33 + j] = acc[c32 * 32 + j];
-          __syncwarp();
-          const int cc = col + c32 * 32;
-          if (cc < P.N) {
-            if (has_epi) {
-              for (int rr = 0; rr < 32; ++rr) {
-                const int row = tc.m0 + q * 32 + rr;
-                if (row >= P.M) break;
-                float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
-                float v = P.alpha * stage[rr * 33 + lane];
-                if (P.beta != 0.f) v += P.beta * *cp;
-                *cp = epilogue_apply(v, P.epi, row);
-              }
-            } else {
-              for (int rr = 0; rr < 32; ++rr) {
-                const int row = tc.m0 + q * 32 + rr;
-                if (row >= P.M) break;
-                float* cp = P.C + static_cast<size_t>(row) * P.ldc + cc;
-                float v = P.alpha * stage[rr * 33 + lane];
-                if (P.beta != 0.f) v += P.beta * *cp;
-                *cp = v;
-              }
-            }
-          }
-          __syncwarp();
-        }
-        continue;
-      }
-      const int row = tc.m0 + q * 32 + lane;
-      if (row < P.M) {
-        float* crow = P.C + static_cast<size_t>(row) * P.ldc;
-        const int col0 = tc.n0 + col_off;
-        const bool vec = ((P.ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(P.C) & 15) == 0);
-        if (has_epi) {
-#pragma unroll
-          for (int j = 0; j < HALF; ++j)
-            if (col0 + j < P.N) {
-              float v = P.alpha * acc[j];
-              if (P.beta != 0.f) v += P.beta * crow[col0 + j];
-              crow[col0 + j] = epilogue_apply(v, P.epi, row);
-            }
-        } else if (vec && col0 + HALF <= P.N) {
-#pragma unroll
-          for (int j = 0; j < HALF; j += 4) {
-            float4 v = make_float4(P.alpha * acc[j], P.alpha * acc[j + 1], P.alpha * acc[j + 2],
-                                   P.alpha * acc[j + 3]);
-            if (P.beta != 0.f) {
-              const float4 o = *reinterpret_cast<const float4*>(crow + col0 + j);
-              v.x += P.beta * o.x; v.y += P.beta * o.y; v.z += P.beta * o.z; v.w += P.beta * o.w;
-            }
-            *reinterpret_cast<float4*>(crow + col0 + j) = v;
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < HALF; ++j)
-            if (col0 + j < P.N) {
-              float v = P.alpha * acc[j];
-              if (P.beta != 0.f) v += P.beta * crow[col0 + j];
-              crow[col0 + j] = v;
-            }
-        }
-      }
+      epi_store<NP, BN, GROUPED, EPI>(P, tc, acc, warp, lane,
+                                      reinterpret_cast<float*>(smem + RING + 256));
     }
   }
 
@@ -580,6 +617,16 @@ __device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t 
   float2 rem = make_float2(x0, x1);
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
+    if (NP == 3 && p == 2) {
+      // what is left after two bf16 pieces has at most 8 significant bits
+      // (x0 takes the top 8 of x's 24, x1 the top 8 of the <= 16 left), so
+      // its upper half is already the bf16 value: taken without a
+      // conversion instruction (those issue at a fraction of the FP32 rate).
+      // It differs from rounding only below bf16's normal range (|r| <
+      // 2^-126), by less than 2^-133.
+      out[p] = __byte_perm(__float_as_uint(rem.x), __float_as_uint(rem.y), 0x7632);
+      break;
+    }
     const __nv_bfloat162 two = __float22bfloat162_rn(rem);
     out[p] = *reinterpret_cast<const uint32_t*>(&two);
     if (p + 1 < NP) {
@@ -1036,13 +1083,16 @@ __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob
 // contiguous is [32][rows] floats, unswizzled.  Converter thread ct takes 8-k
 // chunks (row, c), k in [8c, 8c + 8): along rows where the tile is [32][rows]
 // (consecutive threads read consecutive words), else four chunks of a row
-// per four threads (each reads two 16-byte units).  It splits each value into
-// three bf16 pieces as the pre-pass does and stores them as 16-byte rows of
-// the three planes at the 64-byte-swizzled position the piece copies would
-// have had (byte offset r * 64 + 16 c, its 16-byte unit index XORed with
-// bits 1-2 of the row), then makes its stores visible to the tensor core
-// (fence.proxy.async) and arrives on the piece stage's full barrier and the
-// raw stage's empty barrier.
+// per four threads (each reads two 16-byte units).  It first loads all of
+// its chunks of the stage into registers and releases the raw stage (so the
+// next copy can land while it converts), then waits for the piece stage,
+// splits each value into three bf16 pieces as the pre-pass does and stores
+// them as 16-byte rows of the three planes at the 64-byte-swizzled position
+// the piece copies would have had (byte offset r * 64 + 16 c, its 16-byte
+// unit index XORed with bits 1-2 of the row), then makes its stores visible
+// to the tensor core (fence.proxy.async) and arrives on the piece stage's
+// full barrier.  (Loading a stage's chunks two at a time between stores
+// left each load's latency exposed: 13% slower at 4096^3.)
 template <int NP, int BN>
 __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                               uint8_t* pieces, uint8_t* raw, uint64_t* full, uint64_t* empty,
@@ -1051,8 +1101,10 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
   constexpr int CH_A = kTcBM * (kTcKB / 8);
   constexpr int CH = CH_A + BN * (kTcKB / 8);
   constexpr int PER = (CH + kTcConvThreads - 1) / kTcConvThreads;
-  static_assert(CH_A % 32 == 0, "a warp's chunks are all of one operand");
-  static_assert(kTcKB == 32, "32-deep stages: 128-byte raw rows, 64-byte piece rows");
+  static_assert(CH_A % 32 == 0 && kTcConvThreads % 32 == 0,
+                "a warp's chunks are all of one operand");
+  static_assert(kTcKB == 32 && S::RAW_K == kTcKB,
+                "32-deep stages: 128-byte raw rows, 64-byte piece rows");
   const int4 range = tiles[blockIdx.x];
   uint32_t it = 0;
   for (int t = range.x; t < range.y; ++t) {
@@ -1061,58 +1113,291 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
     const int nkb = P.nkb, kc_a = P.kc_a, kc_b = P.kc_b;
     for (int kb = 0; kb < nkb; ++kb, ++it) {
       const int rs = it % kTcRawStages, ps = it % kTcFusedPieceStages;
-      const bool got = mbar_wait(&raw_full[rs], (it / kTcRawStages) & 1, err, kDevTimeoutFull) &&
-                       mbar_wait(&empty[ps], ((it / kTcFusedPieceStages) & 1) ^ 1, err,
-                                 kDevTimeoutEmpty);
-      if (!__all_sync(0xffffffffu, got)) return;
+      if (!__all_sync(0xffffffffu,
+                      mbar_wait(&raw_full[rs], (it / kTcRawStages) & 1, err, kDevTimeoutFull)))
+        return;
       const uint8_t* ra = raw + rs * S::RAW_BYTES;
+      float v[PER][8];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int ch = ct + kTcConvThreads * i;
+        if (CH % kTcConvThreads != 0 && ch >= CH) continue;
+        const bool is_a = ch < CH_A;
+        const int local = is_a ? ch : ch - CH_A, nrows = is_a ? kTcBM : BN;
+        const uint8_t* src = is_a ? ra : ra + S::RAW_A;
+        if (is_a ? kc_a : kc_b) {  // [rows][32] floats, 128-byte swizzle
+          const int r = local >> 2, c = local & 3;
+          const uint8_t* row = src + r * 128;
+          const float4 lo = *reinterpret_cast<const float4*>(row + (((2 * c) ^ (r & 7)) << 4));
+          const float4 hi = *reinterpret_cast<const float4*>(row + (((2 * c + 1) ^ (r & 7)) << 4));
+          v[i][0] = lo.x; v[i][1] = lo.y; v[i][2] = lo.z; v[i][3] = lo.w;
+          v[i][4] = hi.x; v[i][5] = hi.y; v[i][6] = hi.z; v[i][7] = hi.w;
+        } else {  // [32][rows] floats
+          const int r = local % nrows, c = local / nrows;
+          const float* col = reinterpret_cast<const float*>(src) + (8 * c) * nrows + r;
+#pragma unroll
+          for (int e = 0; e < 8; ++e) v[i][e] = col[e * nrows];
+        }
+      }
+      // the loads are done (the arrive releases them): the copy of a later
+      // stage may overwrite the raw stage now
+      mbar_arrive(&raw_empty[rs]);
+      if (!__all_sync(0xffffffffu, mbar_wait(&empty[ps], ((it / kTcFusedPieceStages) & 1) ^ 1,
+                                              err, kDevTimeoutEmpty)))
+        return;
       uint8_t* pa = pieces + ps * S::STAGE_BYTES;
-      // two chunks at a time, both loaded before either is stored (the
-      // compiler cannot tell the raw and piece rings apart)
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const int ch = ct + kTcConvThreads * i;
+        if (CH % kTcConvThreads != 0 && ch >= CH) continue;
+        const bool is_a = ch < CH_A;
+        const int local = is_a ? ch : ch - CH_A, nrows = is_a ? kTcBM : BN;
+        const bool kc = is_a ? kc_a : kc_b;
+        const int r = kc ? local >> 2 : local % nrows, c = kc ? local & 3 : local / nrows;
+        uint32_t packed[NP][4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          uint32_t two[NP];
+          pieces_pair<NP, 0>(v[i][e], v[i][e + 1], 0, two);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
+        }
+        uint8_t* base = is_a ? pa : pa + S::A_BYTES;
+        const int plane = is_a ? S::A_PLANE : S::B_PLANE;
+        const uint32_t off = static_cast<uint32_t>(r) * 64 + ((c ^ ((r >> 1) & 3)) << 4);
+#pragma unroll
+        for (int p = 0; p < NP; ++p)
+          *reinterpret_cast<uint4*>(base + p * plane + off) =
+              make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+      }
+      fence_proxy_async();
+      mbar_arrive(&full[ps]);
+    }
+  }
+}
+
+
+// Final epilogue of a fused 256-wide tile (the use-th of this CTA), in two
+// halves of the warp's 128 columns so that no more than 64 sums are in
+// registers at once: per half, the drained chunk sums (for the first half
+// read while the last MMAs run), then the last main chunk and the
+// corrections -- the order of the other launches, so the same bits -- the
+// first half parked in `stage` (this warp's 32 x 65 floats of the piece
+// stage that no MMA reads until the warps convert into it again), then TMEM
+// is released and both halves stored: rows of 32 consecutive columns per
+// store instruction, or for a transposed problem (swap: the kernel row is a
+// C column) 32 consecutive floats of one C row.  P is a copy: fields read
+// through a pointer to the problem table would be reloaded after every
+// store to C (the compiler cannot rule out that they alias).
+template <int NP, int BN, bool EPI>
+__device__ __forceinline__ bool fused_dual_finish(const TcProblem P, const TileCoord& tc,
+                                                  const float* sums, uint32_t t_acc,
+                                                  uint64_t* tile_full, uint64_t* tmem_empty,
+                                                  uint64_t* stage_free, uint32_t use,
+                                                  int chunk_kb, int warp, int lane, float* stage,
+                                                  int* err) {
+  constexpr int HALF = BN / 2, Q = HALF / 2;
+  const int ew = warp - 2, q = warp & 3, col_off = (ew >> 2) * HALF;
+  const int n_live = P.N - tc.n0 - col_off;
+  const bool drained = P.nkb > chunk_kb;
+  float a[Q];
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+#pragma unroll
+    for (int j = 0; j < Q; ++j)
+      a[j] = drained && half * Q + j < n_live ? sums[(half * Q + j) * 32] : 0.f;
+    if (half == 0) {
+      if (!__all_sync(0xffffffffu, mbar_wait(&tile_full[0], use & 1, err, kDevTimeoutAccum)))
+        return false;
+      tc_fence_after();
+    }
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+#pragma unroll
+      for (int c16 = 0; c16 < Q / 16; ++c16) {
+        if (half * Q + c16 * 16 >= n_live) break;
+        uint32_t r[16];
+        tmem_ld_32x32b_x16(t_acc + part * BN + half * Q + c16 * 16, r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) a[c16 * 16 + j] += __uint_as_float(r[j]);
+      }
+    }
+    if (half == 0) {
+#pragma unroll
+      for (int j = 0; j < Q; ++j) stage[lane * 65 + j] = a[j];
+    }
+  }
+  tc_fence_before();
+  __syncwarp();
+  if (lane == 0) mbar_arrive(&tmem_empty[0]);
+  const bool has_epi = EPI && (P.epi.bias != nullptr || P.epi.act != 0);
+  const int row0 = tc.m0 + q * 32;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    if (half == 1) {  // the second half goes through the same staging rows
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < Q; ++j) stage[lane * 65 + j] = a[j];
+    }
+    __syncwarp();
+    const int c_base = tc.n0 + col_off + half * Q;  // first kernel column of the half
+    if (P.swap) {
+      const int r = row0 + lane;
+      if (r < P.M) {
+#pragma unroll 8
+        for (int j = 0; j < Q; ++j) {
+          const int c = c_base + j;
+          if (c < P.N) {
+            float* cp = P.C + static_cast<size_t>(c) * P.ldc + r;
+            float v = P.alpha * stage[lane * 65 + j];
+            if (P.beta != 0.f) v += P.beta * *cp;
+            if (has_epi) v = epilogue_apply(v, P.epi, c);
+            *cp = v;
+          }
+        }
+      }
+      continue;
+    }
+#pragma unroll
+    for (int c32 = 0; c32 < Q / 32; ++c32) {
+      const int c = c_base + c32 * 32 + lane;
+      if (c < P.N) {
+        for (int rr = 0; rr < 32; ++rr) {
+          const int row = row0 + rr;
+          if (row >= P.M) break;
+          float* cp = P.C + static_cast<size_t>(row) * P.ldc + c;
+          float v = P.alpha * stage[rr * 65 + c32 * 32 + lane];
+          if (P.beta != 0.f) v += P.beta * *cp;
+          if (has_epi) v = epilogue_apply(v, P.epi, row);
+          *cp = v;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (lane == 0) mbar_arrive(stage_free);  // this warp no longer reads `stage`
+  return true;
+}
+
+// The eight epilogue warps of a 256-wide fused launch, which convert too
+// (ten warps in all, at most 168 registers each: three warps share one
+// scheduler's 16K registers).  Each piece stage comes from two 16-deep raw
+// stages: a tile whose source has k contiguous is [rows][16] floats in
+// 64-byte rows with the 64-byte swizzle (16-byte unit u of row r at
+// u ^ ((r >> 1) & 3)), one whose source has rows contiguous is [16][rows]
+// floats.  Thread ct (0..255) converts three 8-k chunks of each raw stage:
+// one of the a tile (row ct / 2, or column-major position ct), two of the b
+// tile, loaded first and the raw stage released before converting, as in
+// fused_convert.  A 128 x 256 accumulator would take 128 registers of every
+// thread, so the drained chunks of the main accumulator are summed in the
+// CTA's 128 KB of `chunk_sums` (L2-resident; laid out so that a warp's
+// access to one column is 32 consecutive floats) rather than in registers;
+// the sums are added in the order the other launches use, so the results
+// are the same bits.  Between stages the warps do their epilogue work in an
+// order that lets the MMA issuer run ahead: a chunk is drained after the
+// first stage of the next chunk has been converted, and a tile's final
+// epilogue (TMEM read, release, stores) runs after the first stage of the
+// next tile has been converted, so the MMAs of that stage can start as soon
+// as the accumulators are released.  TMEM holds one tile (main + correction
+// accumulators, 2 x 256 columns).
+template <int NP, int BN, bool EPI>
+__device__ void fused_dual(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
+                           float* chunk_sums, uint8_t* smem, uint32_t tmem, uint64_t* full,
+                           uint64_t* empty, uint64_t* raw_full, uint64_t* raw_empty,
+                           uint64_t* main_full, uint64_t* main_empty, uint64_t* tile_full,
+                           uint64_t* tmem_empty, uint64_t* stage_free, int chunk_kb, int warp,
+                           int lane, int* err) {
+  using S = TcShape<NP, BN, false>;
+  constexpr int HALF = BN / 2;
+  constexpr int SUB = kTcKB / S::RAW_K;  // raw stages per piece stage
+  constexpr int CPR = S::RAW_K / 8;      // 8-k chunks per row of a raw stage
+  constexpr int CH_A = kTcBM * CPR;
+  constexpr int CH = CH_A + BN * CPR;
+  constexpr int NT = fused_conv_threads(BN);
+  constexpr int PER = CH / NT;
+  static_assert(S::ACC_BUFS == 1 && SUB == 2 && CPR == 2, "256-wide fused tiles");
+  static_assert(CH % NT == 0 && CH_A == NT, "pass 0 converts the a tile, the others the b tile");
+  static_assert(size_t(kTcEpiWarps) * HALF * 32 * 4 == kTcFusedSumBytes, "chunk sum layout");
+  const int ew = warp - 2, ct = ew * 32 + lane;
+  const int q = warp & 3, col_off = (ew >> 2) * HALF;
+  const uint32_t t_acc = tmem + (static_cast<uint32_t>(q * 32) << 16) + col_off;
+  uint8_t* raw = smem + kTcFusedPieceStages * S::STAGE_BYTES;
+  static_assert(size_t(kTcEpiWarps) * 32 * 65 * 4 <= size_t(S::STAGE_BYTES),
+                "the final epilogue stages half a tile in a piece stage");
+  // this thread's column j of the chunk sums: sums[j * 32]
+  float* sums = chunk_sums + (size_t(blockIdx.x) * kTcEpiWarps + ew) * HALF * 32 + lane;
+  const int4 range = tiles[blockIdx.x];
+  uint32_t it = 0, rit = 0, nbound = 0, ntile = 0;
+  uint32_t nfin = 0, nfin_seen = 0;    // final epilogues done, and waited for
+  int4 pend = make_int4(-1, 0, 0, 0);  // tile record whose final epilogue is due
+
+
+  for (int t = range.x; t < range.y; ++t) {
+    const int4 rec = tiles[gridDim.x + t];
+    const int nkb = probs[rec.x].nkb, kc_a = probs[rec.x].kc_a, kc_b = probs[rec.x].kc_b;
+    for (int kb = 0; kb < nkb; ++kb, ++it) {
+      const int ps = it % kTcFusedPieceStages;
+      uint8_t* pa = smem + ps * S::STAGE_BYTES;
 #pragma unroll 1
-      for (int i = 0; i < PER; i += 2) {
-        float v[2][8];
-        int r[2], c[2];
-        bool live[2], is_a[2];
+      for (int h = 0; h < SUB; ++h, ++rit) {
+        const int rs = rit % kTcRawStages;
+        if (!__all_sync(0xffffffffu, mbar_wait(&raw_full[rs], (rit / kTcRawStages) & 1, err,
+                                                kDevTimeoutFull)))
+          return;
+        const uint8_t* ra = raw + rs * S::RAW_BYTES;
+        float v[PER][8];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int ch = ct + kTcConvThreads * (i + u);
-          live[u] = i + u < PER && (CH % kTcConvThreads == 0 || ch < CH);
-          is_a[u] = ch < CH_A;
-          if (!live[u]) continue;
-          const int local = is_a[u] ? ch : ch - CH_A, nrows = is_a[u] ? kTcBM : BN;
-          const uint8_t* src = is_a[u] ? ra : ra + S::RAW_A;
-          if (is_a[u] ? kc_a : kc_b) {  // [rows][32] floats, 128-byte swizzle
-            r[u] = local >> 2;
-            c[u] = local & 3;
-            const uint8_t* row = src + r[u] * 128;
-            const float4 lo = *reinterpret_cast<const float4*>(row + (((2 * c[u]) ^ (r[u] & 7)) << 4));
-            const float4 hi =
-                *reinterpret_cast<const float4*>(row + (((2 * c[u] + 1) ^ (r[u] & 7)) << 4));
-            v[u][0] = lo.x; v[u][1] = lo.y; v[u][2] = lo.z; v[u][3] = lo.w;
-            v[u][4] = hi.x; v[u][5] = hi.y; v[u][6] = hi.z; v[u][7] = hi.w;
-          } else {   // [32][rows] floats
-            r[u] = local % nrows;
-            c[u] = local / nrows;
-            const float* col = reinterpret_cast<const float*>(src) + (8 * c[u]) * nrows + r[u];
+        for (int i = 0; i < PER; ++i) {
+          const bool is_a = i == 0;
+          const int local = is_a ? ct : ct + NT * i - CH_A, nrows = is_a ? kTcBM : BN;
+          const uint8_t* src = is_a ? ra : ra + S::RAW_A;
+          if (is_a ? kc_a : kc_b) {  // [rows][16] floats, 64-byte swizzle
+            const int r = local / CPR, c = local % CPR, sw = (r >> 1) & 3;
+            const uint8_t* row = src + r * (S::RAW_K * 4);
+            const float4 lo = *reinterpret_cast<const float4*>(row + (((2 * c) ^ sw) << 4));
+            const float4 hi = *reinterpret_cast<const float4*>(row + (((2 * c + 1) ^ sw) << 4));
+            v[i][0] = lo.x; v[i][1] = lo.y; v[i][2] = lo.z; v[i][3] = lo.w;
+            v[i][4] = hi.x; v[i][5] = hi.y; v[i][6] = hi.z; v[i][7] = hi.w;
+          } else {  // [16][rows] floats
+            const int r = local % nrows, c = local / nrows;
+            const float* col = reinterpret_cast<const float*>(src) + (8 * c) * nrows + r;
 #pragma unroll
-            for (int e = 0; e < 8; ++e) v[u][e] = col[e * nrows];
+            for (int e = 0; e < 8; ++e) v[i][e] = col[e * nrows];
+          }
+        }
+        mbar_arrive(&raw_empty[rs]);  // the loads are done (released by the arrive)
+        if (h == 0) {
+          if (!__all_sync(0xffffffffu, mbar_wait(&empty[ps], ((it / kTcFusedPieceStages) & 1) ^ 1,
+                                                 err, kDevTimeoutEmpty)))
+            return;
+          // the stage after a tile's final epilogue held that epilogue's
+          // parked sums: every warp must be done with them
+          if (nfin != nfin_seen) {
+            if (!__all_sync(0xffffffffu,
+                            mbar_wait(stage_free, (nfin - 1) & 1, err, kDevTimeoutAccum)))
+              return;
+            nfin_seen = nfin;
           }
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          if (!live[u]) continue;
+        for (int i = 0; i < PER; ++i) {
+          const bool is_a = i == 0;
+          const int local = is_a ? ct : ct + NT * i - CH_A, nrows = is_a ? kTcBM : BN;
+          const bool kc = is_a ? kc_a : kc_b;
+          const int r = kc ? local / CPR : local % nrows;
+          const int c = h * CPR + (kc ? local % CPR : local / nrows);  // 8-k chunk of the stage
           uint32_t packed[NP][4];
 #pragma unroll
           for (int e = 0; e < 8; e += 2) {
             uint32_t two[NP];
-            pieces_pair<NP, 0>(v[u][e], v[u][e + 1], 0, two);
+            pieces_pair<NP, 0>(v[i][e], v[i][e + 1], 0, two);
 #pragma unroll
             for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
           }
-          uint8_t* base = is_a[u] ? pa : pa + S::A_BYTES;
-          const int plane = is_a[u] ? S::A_PLANE : S::B_PLANE;
-          const uint32_t off = static_cast<uint32_t>(r[u]) * 64 + ((c[u] ^ ((r[u] >> 1) & 3)) << 4);
+          uint8_t* base = is_a ? pa : pa + S::A_BYTES;
+          const int plane = is_a ? S::A_PLANE : S::B_PLANE;
+          const uint32_t off = static_cast<uint32_t>(r) * 64 + ((c ^ ((r >> 1) & 3)) << 4);
 #pragma unroll
           for (int p = 0; p < NP; ++p)
             *reinterpret_cast<uint4*>(base + p * plane + off) =
@@ -1121,9 +1406,63 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
       }
       fence_proxy_async();
       mbar_arrive(&full[ps]);
-      mbar_arrive(&raw_empty[rs]);
+      if (kb == 0) {
+        // the piece stage after the one just converted is free: the last
+        // MMAs that read it belong to the finished tile
+        if (pend.x >= 0 &&
+            !fused_dual_finish<NP, BN, EPI>(
+                probs[pend.x], TileCoord{pend.x, pend.y, pend.z}, sums, t_acc, tile_full,
+                tmem_empty, stage_free, ntile - 1, chunk_kb, warp, lane,
+                reinterpret_cast<float*>(smem + ((it + 1) % kTcFusedPieceStages) * S::STAGE_BYTES) +
+                    ew * 32 * 65,
+                err))
+          return;
+        if (pend.x >= 0) ++nfin;
+      } else if (kb % chunk_kb == 0) {
+        // the chunk that ended at stage kb - 1: the tile's first one is
+        // stored, later ones added (TMEM read half a warp's columns at a
+        // time; the accumulator is released once all of it is read)
+        if (!__all_sync(0xffffffffu, mbar_wait(&main_full[0], nbound & 1, err, kDevTimeoutAccum)))
+          return;
+        ++nbound;
+        tc_fence_after();
+        const int n_live = probs[rec.x].N - rec.z - col_off;
+        const bool first = kb == chunk_kb;
+        // 32 columns at a time: the old sums are loaded together (one L2
+        // round trip per slice, not one per column) while TMEM is read
+#pragma unroll
+        for (int c32 = 0; c32 < HALF / 32; ++c32) {
+          float old[32];
+          uint32_t r[32];
+          const bool live = c32 * 32 < n_live;
+          if (live) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] = first ? 0.f : sums[(c32 * 32 + j) * 32];
+            tmem_ld_32x32b_x32(t_acc + c32 * 32, r);
+            tmem_ld_wait();
+          }
+          if (c32 == HALF / 32 - 1) {  // all of the chunk read: release it
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&main_empty[0]);
+          }
+          if (live) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (c32 * 32 + j < n_live) sums[(c32 * 32 + j) * 32] = old[j] + __uint_as_float(r[j]);
+          }
+        }
+      }
     }
+    pend = rec;
+    ++ntile;
   }
+  if (pend.x >= 0)
+    fused_dual_finish<NP, BN, EPI>(
+        probs[pend.x], TileCoord{pend.x, pend.y, pend.z}, sums, t_acc, tile_full, tmem_empty,
+        stage_free, ntile - 1, chunk_kb, warp, lane,
+        reinterpret_cast<float*>(smem + (it % kTcFusedPieceStages) * S::STAGE_BYTES) + ew * 32 * 65,
+        err);
 }
 
 template <int NP, int FMT>
@@ -1159,7 +1498,7 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
   if (!smem_attr_once(kern, kSmem, attr_done)) return UGEMM_ERR_CUDA;
   const int grid = std::max(1, std::min(total_tiles, max_ctas > 0 ? max_ctas : sm_count()));
   prof_begin(st);
-  kern<<<grid, FUSED ? kTcFusedThreads : kTcThreads, kSmem, st>>>(
+  kern<<<grid, FUSED ? fused_threads(BN) : kTcThreads, kSmem, st>>>(
       ta, tb, single, maps, probs, tiles, total_tiles, nprod, chunk_kb, fmt, dev_err);
   prof_end(st, GROUPED ? kProfGrouped : kProfSplitGemm);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
@@ -1337,14 +1676,20 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                int chunk_kb,
                                int max_ctas, int* dev_err, cudaStream_t st) {
   const bool grouped = probs != nullptr;
-  if (p.fused) {  // grouped launches of three bf16 pieces in 128-wide tiles only
-    if (p.pieces != 3 || p.block_n != 128 || !grouped) return UGEMM_ERR_ARG;
-    return p.epi ? launch_kernel<3, 128, true, true, false, true>(
-                       ta, tb, single, maps, probs, tiles, total_tiles, p.products, chunk_kb,
-                       max_ctas, 0, dev_err, st)
-                 : launch_kernel<3, 128, true, false, false, true>(
-                       ta, tb, single, maps, probs, tiles, total_tiles, p.products, chunk_kb,
-                       max_ctas, 0, dev_err, st);
+  if (p.fused) {  // grouped launches of three bf16 pieces only
+    if (p.pieces != 3 || !grouped || (p.block_n == 256 && single.chunk_sums == nullptr))
+      return UGEMM_ERR_ARG;
+#define UGEMM_FUSED_CASE(BN, EPI)                                                                \
+  if (p.block_n == BN && p.epi == EPI)                                                          \
+    return launch_kernel<3, BN, true, EPI, false, true>(ta, tb, single, maps, probs, tiles,     \
+                                                        total_tiles, p.products, chunk_kb,      \
+                                                        max_ctas, 0, dev_err, st);
+    UGEMM_FUSED_CASE(128, false)
+    UGEMM_FUSED_CASE(128, true)
+    UGEMM_FUSED_CASE(256, false)
+    UGEMM_FUSED_CASE(256, true)
+#undef UGEMM_FUSED_CASE
+    return UGEMM_ERR_ARG;
   }
   const int fmt = p.f16 ? 1 : 0;
   const bool tf32 = p.pieces == kPiecesTf32;
@@ -1395,14 +1740,18 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
 int split_kp(int K) { return kp_of(K); }
 
 bool fused_encode_map(const float* base, long long ld, int R, int Cc, bool kcontig, int box_rows,
-                      CUtensorMap* map) {
+                      int box_k, CUtensorMap* map) {
   if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld & 3) || R < 1 || Cc < 1) return false;
-  // the stored matrix: R rows of Cc floats; the box is 32 k by box_rows rows
-  // of the kernel operand, k along the columns (kcontig) or along the rows
+  if (box_k != kTcKB && box_k != kTcKB / 2) return false;
+  // the stored matrix: R rows of Cc floats; the box is box_k k by box_rows
+  // rows of the kernel operand, k along the columns (kcontig: rows of
+  // 4 * box_k bytes, swizzled over that width) or along the rows
   return kcontig ? encode_tmap_2d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, Cc, R, ld * 4ull,
-                                  kTcKB, box_rows, CU_TENSOR_MAP_SWIZZLE_128B)
+                                  box_k, box_rows,
+                                  box_k == kTcKB ? CU_TENSOR_MAP_SWIZZLE_128B
+                                                 : CU_TENSOR_MAP_SWIZZLE_64B)
                  : encode_tmap_2d(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, Cc, R, ld * 4ull,
-                                  box_rows, kTcKB, CU_TENSOR_MAP_SWIZZLE_NONE);
+                                  box_rows, box_k, CU_TENSOR_MAP_SWIZZLE_NONE);
 }
 
 }  // namespace ugemm

@@ -17,15 +17,31 @@ constexpr int kTcEpiWarps = 8;   // two per TMEM lane quarter
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
 // Fused launches (the operands split inside the GEMM kernel): warp 0's TMA
 // copies bring raw FP32 tiles of the operands into a ring of kTcRawStages
-// stages, and kTcConvWarps more warps after the epilogue warps (six: sixteen
-// warps in all, 128 registers each) convert each
-// into the three bf16 pieces of a piece stage (kTcFusedPieceStages of them),
-// which the MMA issuer reads as it reads pre-split pieces.
+// stages, which converter threads split into the three bf16 pieces of a
+// piece stage (kTcFusedPieceStages of them); the MMA issuer reads those as
+// it reads pre-split pieces.  128-wide tiles: kTcConvWarps more warps after
+// the epilogue warps (six: sixteen warps in all, 128 registers each), raw
+// stages 32 k deep.  256-wide tiles: the accumulator of a 128 x 256 tile
+// needs 128 registers in each epilogue thread, so there is no register room
+// for more warps; the eight epilogue warps convert as well (ten warps, up to
+// 200 registers each), and the raw stages are 16 k deep, so that two piece
+// stages and three raw stages fit in shared memory.
 constexpr int kTcConvWarps = 6;
 constexpr int kTcConvThreads = kTcConvWarps * 32;
 constexpr int kTcFusedThreads = kTcThreads + kTcConvThreads;
 constexpr int kTcFusedPieceStages = 2;
 constexpr int kTcRawStages = 3;
+// threads, converter threads and raw stage depth of a fused launch
+__host__ __device__ constexpr int fused_threads(int bn) {
+  return bn == 256 ? kTcThreads : kTcFusedThreads;
+}
+__host__ __device__ constexpr int fused_conv_threads(int bn) {
+  return bn == 256 ? kTcEpiWarps * 32 : kTcConvThreads;
+}
+__host__ __device__ constexpr int fused_raw_k(int bn) { return bn == 256 ? kTcKB / 2 : kTcKB; }
+// 256-wide fused launches keep the drained chunks of the main accumulator
+// in global memory (L2) instead of registers: 128 x 256 FP32 per CTA.
+constexpr size_t kTcFusedSumBytes = size_t(kTcBM) * 256 * 4;
 constexpr int kTcRaster = 8;     // tile rows per raster group (L2 reuse)
 
 // FP16x3 form: every row of an operand's K-major piece matrix -- a row of
@@ -104,9 +120,10 @@ struct TcShape {
   static constexpr size_t SMEM =
       1024 + size_t(STAGES) * STAGE_BYTES + 256 + STAGE_C_BYTES + STAGE_C8_BYTES;
   // fused launches: kTcFusedPieceStages piece stages, then kTcRawStages raw
-  // FP32 stages (the a tile, then the b tile, 32 k deep)
-  static constexpr int RAW_A = kTcBM * kTcKB * 4;
-  static constexpr int RAW_BYTES = RAW_A + BN * kTcKB * 4;
+  // FP32 stages (the a tile, then the b tile, RAW_K deep)
+  static constexpr int RAW_K = fused_raw_k(BN);
+  static constexpr int RAW_A = kTcBM * RAW_K * 4;
+  static constexpr int RAW_BYTES = RAW_A + BN * RAW_K * 4;
   static constexpr size_t FUSED_RING =
       size_t(kTcFusedPieceStages) * STAGE_BYTES + size_t(kTcRawStages) * RAW_BYTES;
   static constexpr size_t SMEM_FUSED = 1024 + FUSED_RING + 256 + STAGE_C_BYTES + STAGE_C8_BYTES;
@@ -146,6 +163,9 @@ struct TcProblem {
   // contiguous (box {rows, 32 k}, no swizzle); maps[2 * map] and
   // maps[2 * map + 1] then describe the FP32 sources
   int kc_a = 1, kc_b = 1;
+  // fused 256-wide launches (set in the `single` record only): the chunk
+  // sums of the epilogue warps, kTcFusedSumBytes per persistent CTA
+  float* chunk_sums = nullptr;
 };
 
 // One operand to split in the batched pre-pass.
@@ -229,10 +249,11 @@ ugemm_status split_gemm_launch(const SplitPlan& p, const CUtensorMap& ta, const 
                                int chunk_kb, int max_ctas, int* dev_err, cudaStream_t st);
 // The TMA map of a fused launch's FP32 operand stored as R rows x Cc columns
 // (leading dimension ld elements): kcontig, the kernel reads k along the
-// columns (box {32, box_rows}, 128-byte swizzle); else rows along them (box
-// {box_rows, 32}).  False if TMA cannot describe it (alignment).
+// columns (box {box_k, box_rows}; 128-byte swizzle for 32-deep boxes, 64-byte
+// for 16-deep ones); else rows along them (box {box_rows, box_k}).  False if
+// TMA cannot describe it (alignment).
 bool fused_encode_map(const float* base, long long ld, int R, int Cc, bool kcontig, int box_rows,
-                      CUtensorMap* map);
+                      int box_k, CUtensorMap* map);
 // Tile table of a grouped launch of `grid` persistent CTAs: grid ranges
 // {first, end, 0, 0} into the records that follow, one {problem, m0, n0, 0}
 // per tile (raster order within a problem), dealt longest first to the

@@ -190,9 +190,10 @@ UGEMM_API int ugemm_tune_grouped(int count, const ugemm_problem* problems, int p
     // chunk_k <= 256 keeps the split form at least as accurate as FP32 SIMT
     for (int bn : {128, 256})
       for (int ck : {128, 256}) consider(ugemm_tile_config{bn, ck, 0, 0, 0, 0, 0});
-    // three bf16 pieces: the operands split inside the GEMM kernel (128-wide)
+    // three bf16 pieces: the operands split inside the GEMM kernel
     if (form == UGEMM_PREC_BF16X6 || form == UGEMM_PREC_BF16X9)
-      for (int ck : {128, 256}) consider(ugemm_tile_config{128, ck, 0, 0, 0, 0, 1});
+      for (int bn : {128, 256})
+        for (int ck : {128, 256}) consider(ugemm_tile_config{bn, ck, 0, 0, 0, 0, 1});
   }
   // 2. schedule, one knob at a time from the best so far
   if (cur_t < 1e30) {
