@@ -61,10 +61,6 @@
 namespace ugemm {
 namespace {
 
-// Correction products in issue order, encoded (ia << 2) | ib; the main
-// product a0*b0 is implicit.
-__constant__ uint8_t kCorrections[8] = {0x1, 0x4, 0x2, 0x5, 0x8, 0x6, 0x9, 0xA};
-
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
   return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
@@ -305,6 +301,110 @@ __device__ void fused_dual(const TcProblem* __restrict__ probs, const int4* __re
                            uint64_t* tmem_empty, uint64_t* stage_free, int chunk_kb, int warp,
                            int lane, int* err);
 
+// Correction products in issue order, (a piece << 2) | b piece; the main
+// product a0*b0 is issued after them.
+__host__ __device__ constexpr uint32_t corr_code(int p) {
+  return p == 0 ? 0x1 : p == 1 ? 0x4 : p == 2 ? 0x2 : p == 3 ? 0x5 : p == 4 ? 0x8
+       : p == 5 ? 0x6 : p == 6 ? 0x9 : 0xA;
+}
+
+// The MMA issuer (one thread).  Per k-block: wait for the stage, issue the
+// correction products into their accumulator, the main product into its
+// (restarted at each chunk once the epilogue drained it), commit the stage
+// free; per tile, commit the accumulators full.  Everything per k-block is
+// compile-time but the stage: the descriptors are those of stage 0 plus the
+// stage's offset (the address field counts 16-byte units, and shared
+// memory stays below 256 KB, so the field never carries), the product
+// count is a template parameter, and the chunk position is a counter
+// rather than a remainder (a run-time division cost ~400 cycles per
+// k-block in the issuing thread, a gap in which the tensor pipe drained).
+template <int NP, int BN, bool GROUPED, bool TF32, bool FUSED, int NPROD>
+__device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
+                                               const TcProblem* __restrict__ probs,
+                                               const int4* __restrict__ tiles, int total_tiles,
+                                               uint8_t* smem, uint32_t tmem, uint64_t* full,
+                                               uint64_t* empty, uint64_t* main_full,
+                                               uint64_t* main_empty, uint64_t* tile_full,
+                                               uint64_t* tmem_empty, int chunk_kb, int fmt,
+                                               int* err) {
+  constexpr bool WIDE = split_stage_k(NP) > kTcKB;
+  using S = TcShape<NP, BN, WIDE>;
+  constexpr int KK = S::KB / 16;  // k steps of 32 bytes per row in a stage
+  constexpr uint32_t SBO = WIDE ? 1024 : 512, SWZ = WIDE ? 2 : 4;
+  constexpr int NST = FUSED ? kTcFusedPieceStages : S::STAGES;
+  constexpr int NB = S::ACC_BUFS;
+  // instruction descriptor operand format: bf16 pieces (1), the FP16x3
+  // form's fp16 pieces (0) or the TF32x3 form's tf32 pieces (2); one k step
+  // is 32 bytes of a row in each: 16 16-bit or 8 tf32 elements
+  const uint32_t ifmt = TF32 ? 2u : (NP == 2 && fmt == 1 ? 0u : 1u);
+  const uint32_t idesc_full = umma_idesc(ifmt, ifmt, kTcBM, BN);
+  const uint32_t base = smem_u32(smem);
+  const uint64_t da0 = umma_smem_desc(base, SBO, SWZ);
+  const uint64_t db0 = umma_smem_desc(base + S::A_BYTES, SBO, SWZ);
+  uint32_t s = 0, ph = 0, ntile = 0;
+  uint32_t nbound[NB] = {};
+  const TileRange tr = tile_range<GROUPED>(tiles, total_tiles);
+  for (int t = tr.first; t < tr.end; t += tr.step, ++ntile) {
+    TcProblem P;
+    const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, tiles, t, P);
+    // a group's narrow problems and right-edge tiles multiply only the
+    // columns that exist (UMMA N in steps of 16)
+    uint32_t idesc = idesc_full;
+    if constexpr (GROUPED) {
+      const int n_rem = P.N - tc.n0;
+      if (n_rem < BN)
+        idesc = umma_idesc(ifmt, ifmt, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
+    }
+    const uint32_t buf = NB == 1 ? 0u : ntile % NB, use = ntile / NB;
+    const uint32_t t_main = tmem + buf * 2 * BN, t_corr = t_main + BN;
+    // the epilogue must have read this buffer's previous tile
+    if (use > 0 && !mbar_wait(&tmem_empty[buf], (use - 1) & 1, err, kDevTimeoutAccum)) return;
+    tc_fence_after();
+    int cpos = 0;  // the k-block's position in its chunk
+    for (int kb = 0; kb < P.nkb; ++kb) {
+      if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) return;
+      tc_fence_after();
+      const uint64_t so = (s * static_cast<uint32_t>(S::STAGE_BYTES)) >> 4;
+      const uint64_t da = da0 + so, db = db0 + so;
+      // correction products into their own accumulator
+#pragma unroll
+      for (int p = 0; p < NPROD - 1; ++p) {
+        const uint32_t ia = corr_code(p) >> 2, ib = corr_code(p) & 3;
+#pragma unroll
+        for (int kk = 0; kk < KK; ++kk) {
+          const uint64_t a = da + ((ia * S::A_PLANE + kk * 32) >> 4);
+          const uint64_t b = db + ((ib * S::B_PLANE + kk * 32) >> 4);
+          if constexpr (TF32) umma_tf32(t_corr, a, b, idesc, (kb | p | kk) != 0);
+          else umma_bf16(t_corr, a, b, idesc, (kb | p | kk) != 0);
+        }
+      }
+      // main product; a new chunk restarts the accumulator once drained
+      const bool chunk_start = cpos == 0;
+      if (chunk_start && kb > 0) {
+        if (!mbar_wait(&main_empty[buf], nbound[buf] & 1, err, kDevTimeoutAccum)) return;
+        ++nbound[buf];
+        tc_fence_after();
+      }
+#pragma unroll
+      for (int kk = 0; kk < KK; ++kk) {
+        const uint64_t a = da + ((kk * 32) >> 4), b = db + ((kk * 32) >> 4);
+        if constexpr (TF32) umma_tf32(t_main, a, b, idesc, !(chunk_start && kk == 0));
+        else umma_bf16(t_main, a, b, idesc, !(chunk_start && kk == 0));
+      }
+      umma_commit(&empty[s]);
+      if (++cpos == chunk_kb) {
+        cpos = 0;
+        if (kb + 1 < P.nkb) umma_commit(&main_full[buf]);
+      }
+      if (++s == NST) {
+        s = 0;
+        ph ^= 1;
+      }
+    }
+    umma_commit(&tile_full[buf]);
+  }
+}
+
 // TF32: the TF32x3 form's instantiation (two planes of 32-deep tf32
 // stages, tcgen05 kind::tf32), a template parameter so that the 16-bit
 // instantiations' MMA issue loop carries no branch on the format.
@@ -461,75 +561,20 @@ __global__ void __launch_bounds__(FUSED ? fused_threads(BN) : kTcThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      // instruction descriptor operand format: bf16 pieces (1), the FP16x3
-      // form's fp16 pieces (0) or the TF32x3 form's tf32 pieces (2); one
-      // k step is 32 bytes of a row in each: 16 16-bit or 8 tf32 elements
-      const uint32_t ifmt = TF32 ? 2u : (NP == 2 && fmt == 1 ? 0u : 1u);
-      const uint32_t idesc_full = umma_idesc(ifmt, ifmt, kTcBM, BN);
-      const uint32_t base = smem_u32(smem);
-      uint32_t it = 0, ntile = 0;
-      uint32_t nbound[NB] = {};
-      bool ok = true;
-      const TileRange tr = tile_range<GROUPED>(tiles, total_tiles);
-      for (int t = tr.first; ok && t < tr.end; t += tr.step, ++ntile) {
-        TcProblem P;
-        const TileCoord tc = tile_coord<BN, GROUPED>(single, probs, tiles, t, P);
-        // a group's narrow problems and right-edge tiles multiply only the
-        // columns that exist (UMMA N in steps of 16)
-        uint32_t idesc = idesc_full;
-        if constexpr (GROUPED) {
-          const int n_rem = P.N - tc.n0;
-          if (n_rem < BN) idesc = umma_idesc(ifmt, ifmt, kTcBM, static_cast<uint32_t>((n_rem + 15) & ~15));
-        }
-        const uint32_t buf = ntile % NB, use = ntile / NB;
-        const uint32_t t_main = tmem + buf * 2 * BN, t_corr = t_main + BN;
-        // the epilogue must have read this buffer's previous tile
-        if (use > 0 && !mbar_wait(&tmem_empty[buf], (use - 1) & 1, err, kDevTimeoutAccum)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        for (int kb = 0; kb < P.nkb; ++kb, ++it) {
-          const int s = it % NST;
-          const uint32_t ph = (it / NST) & 1;
-          if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) { ok = false; break; }
-          tc_fence_after();
-          const uint32_t sa = base + s * S::STAGE_BYTES;
-          const uint32_t sb = sa + S::A_BYTES;
-          // correction products into their own accumulator
-          for (int p = 0; p < nprod - 1; ++p) {
-            const uint32_t code = kCorrections[p];
-            const uint32_t ia = code >> 2, ib = code & 3;
-#pragma unroll
-            for (int kk = 0; kk < KB / 16; ++kk) {
-              const uint64_t da = umma_smem_desc(sa + ia * S::A_PLANE + kk * 32, SBO, SWZ);
-              const uint64_t db = umma_smem_desc(sb + ib * S::B_PLANE + kk * 32, SBO, SWZ);
-              if constexpr (TF32) umma_tf32(t_corr, da, db, idesc, (kb | p | kk) != 0);
-              else umma_bf16(t_corr, da, db, idesc, (kb | p | kk) != 0);
-            }
-          }
-          // main product; a new chunk restarts the accumulator once drained
-          const bool chunk_start = (kb % chunk_kb) == 0;
-          if (chunk_start && kb > 0) {
-            if (!mbar_wait(&main_empty[buf], nbound[buf] & 1, err, kDevTimeoutAccum)) {
-              ok = false;
-              break;
-            }
-            ++nbound[buf];
-            tc_fence_after();
-          }
-#pragma unroll
-          for (int kk = 0; kk < KB / 16; ++kk) {
-            const uint64_t da = umma_smem_desc(sa + kk * 32, SBO, SWZ);
-            const uint64_t db = umma_smem_desc(sb + kk * 32, SBO, SWZ);
-            if constexpr (TF32) umma_tf32(t_main, da, db, idesc, !(chunk_start && kk == 0));
-            else umma_bf16(t_main, da, db, idesc, !(chunk_start && kk == 0));
-          }
-          umma_commit(&empty[s]);
-          if ((kb + 1) % chunk_kb == 0 && kb + 1 < P.nkb) umma_commit(&main_full[buf]);
-        }
-        umma_commit(&tile_full[buf]);
-      }
+      // the product count as a compile-time constant: two-piece forms have
+      // three products, three-piece ones six (BF16x6) or nine (BF16x9)
+      if constexpr (NP == 2)
+        mma_issue_loop<NP, BN, GROUPED, TF32, FUSED, 3>(single, probs, tiles, total_tiles, smem,
+                                                        tmem, full, empty, main_full, main_empty,
+                                                        tile_full, tmem_empty, chunk_kb, fmt, err);
+      else if (nprod == 9)
+        mma_issue_loop<NP, BN, GROUPED, TF32, FUSED, 9>(single, probs, tiles, total_tiles, smem,
+                                                        tmem, full, empty, main_full, main_empty,
+                                                        tile_full, tmem_empty, chunk_kb, fmt, err);
+      else
+        mma_issue_loop<NP, BN, GROUPED, TF32, FUSED, 6>(single, probs, tiles, total_tiles, smem,
+                                                        tmem, full, empty, main_full, main_empty,
+                                                        tile_full, tmem_empty, chunk_kb, fmt, err);
     }
     __syncwarp();
   } else if (DUAL) {
@@ -1084,15 +1129,15 @@ __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob
 // chunks (row, c), k in [8c, 8c + 8): along rows where the tile is [32][rows]
 // (consecutive threads read consecutive words), else four chunks of a row
 // per four threads (each reads two 16-byte units).  It first loads all of
-// its chunks of the stage into registers and releases the raw stage (so the
-// next copy can land while it converts), then waits for the piece stage,
+// its chunks of the stage into registers, then waits for the piece stage,
 // splits each value into three bf16 pieces as the pre-pass does and stores
 // them as 16-byte rows of the three planes at the 64-byte-swizzled position
 // the piece copies would have had (byte offset r * 64 + 16 c, its 16-byte
 // unit index XORed with bits 1-2 of the row), then makes its stores visible
 // to the tensor core (fence.proxy.async) and arrives on the piece stage's
-// full barrier.  (Loading a stage's chunks two at a time between stores
-// left each load's latency exposed: 13% slower at 4096^3.)
+// full barrier and the raw stage's empty barrier.  (Loading a stage's
+// chunks two at a time between stores left each load's latency exposed:
+// 13% slower at 4096^3.)
 template <int NP, int BN>
 __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                               uint8_t* pieces, uint8_t* raw, uint64_t* full, uint64_t* empty,
@@ -1139,9 +1184,6 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
           for (int e = 0; e < 8; ++e) v[i][e] = col[e * nrows];
         }
       }
-      // the loads are done (the arrive releases them): the copy of a later
-      // stage may overwrite the raw stage now
-      mbar_arrive(&raw_empty[rs]);
       if (!__all_sync(0xffffffffu, mbar_wait(&empty[ps], ((it / kTcFusedPieceStages) & 1) ^ 1,
                                               err, kDevTimeoutEmpty)))
         return;
@@ -1170,8 +1212,14 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
           *reinterpret_cast<uint4*>(base + p * plane + off) =
               make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
       }
+      // the stores and the raw loads, ordered before the tensor core reads
+      // the pieces and before the next copy overwrites the raw stage (a
+      // copy is an async-proxy write: releasing the raw stage right after
+      // the loads, without this fence, let copies land in it while its
+      // loads were in flight -- wrong results on the GPU)
       fence_proxy_async();
       mbar_arrive(&full[ps]);
+      mbar_arrive(&raw_empty[rs]);
     }
   }
 }
@@ -1288,8 +1336,8 @@ __device__ __forceinline__ bool fused_dual_finish(const TcProblem P, const TileC
 // u ^ ((r >> 1) & 3)), one whose source has rows contiguous is [16][rows]
 // floats.  Thread ct (0..255) converts three 8-k chunks of each raw stage:
 // one of the a tile (row ct / 2, or column-major position ct), two of the b
-// tile, loaded first and the raw stage released before converting, as in
-// fused_convert.  A 128 x 256 accumulator would take 128 registers of every
+// tile, loaded first, then converted and stored, and the raw stage released
+// after a proxy fence, as in fused_convert.  A 128 x 256 accumulator would take 128 registers of every
 // thread, so the drained chunks of the main accumulator are summed in the
 // CTA's 128 KB of `chunk_sums` (L2-resident; laid out so that a warp's
 // access to one column is 32 consecutive floats) rather than in registers;
@@ -1366,7 +1414,6 @@ __device__ void fused_dual(const TcProblem* __restrict__ probs, const int4* __re
             for (int e = 0; e < 8; ++e) v[i][e] = col[e * nrows];
           }
         }
-        mbar_arrive(&raw_empty[rs]);  // the loads are done (released by the arrive)
         if (h == 0) {
           if (!__all_sync(0xffffffffu, mbar_wait(&empty[ps], ((it / kTcFusedPieceStages) & 1) ^ 1,
                                                  err, kDevTimeoutEmpty)))
@@ -1403,8 +1450,11 @@ __device__ void fused_dual(const TcProblem* __restrict__ probs, const int4* __re
             *reinterpret_cast<uint4*>(base + p * plane + off) =
                 make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
         }
+        // the raw stage's loads and these stores, ordered before the next
+        // copy into the raw stage and the tensor core's reads (async proxy)
+        fence_proxy_async();
+        mbar_arrive(&raw_empty[rs]);
       }
-      fence_proxy_async();
       mbar_arrive(&full[ps]);
       if (kb == 0) {
         // the piece stage after the one just converted is free: the last

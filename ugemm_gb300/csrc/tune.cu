@@ -100,13 +100,13 @@ void store(const std::string& dev, int form, uint64_t sig, const ugemm_tile_conf
   std::fprintf(f,
                "{\"device\": \"%s\", \"form\": %d, \"sig\": \"%016" PRIx64
                "\", \"block_n\": %d, \"chunk_k\": %d, \"max_ctas\": %d, \"split_k\": %d, "
-               "\"deal\": %d, \"transpose\": %d, \"fused\": %d, \"ms\": %.6f, "
+               "\"deal\": %d, \"transpose\": %d, \"fused\": %d, \"ms\": %.9g, "
                "\"candidates\": [",
                dev.c_str(), form, sig, c.block_n, c.chunk_k, c.max_ctas, c.split_k, c.deal,
                c.transpose, c.fused, ms);
   for (size_t i = 0; i < all.size(); ++i) {
     const ugemm_tile_config& x = all[i].c;
-    std::fprintf(f, "%s[%d, %d, %d, %d, %d, %d, %d, %.6f]", i ? ", " : "", x.block_n,
+    std::fprintf(f, "%s[%d, %d, %d, %d, %d, %d, %d, %.9g]", i ? ", " : "", x.block_n,
                  x.chunk_k, x.max_ctas, x.split_k, x.deal, x.transpose, x.fused, all[i].ms);
   }
   std::fprintf(f, "]}\n");
