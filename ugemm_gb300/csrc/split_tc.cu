@@ -30,10 +30,9 @@
 //      (Kp = K rounded up to 32, zero padded);
 //   2. GEMM kernel, 10 warps:
 //        warp 0   TMA producer: one 3-D TMA per operand per stage brings all
-//                 pieces of a 32-deep k slice (64-byte swizzle) into a 3-4
-//                 stage ring (mbarrier full/empty pairs) -- for two-piece
-//                 operands a 64-deep slice (128-byte swizzle) into a 2-3
-//                 stage ring, which halves the per-stage overhead;
+//                 pieces of a 32-deep k slice (64-byte swizzle; TF32
+//                 pieces: 128-byte rows and swizzle) into a 3-4 stage ring
+//                 (mbarrier full/empty pairs);
 //        warp 1   allocates TMEM (2 x BN columns: main + corrections) and,
 //                 from one thread, issues the tcgen05.mma stream;
 //        warps 2-9  epilogue: chunk drains, then alpha/beta and the store of
@@ -119,7 +118,7 @@ template <int NP, int BN, bool GROUPED, bool EPI>
 __device__ __forceinline__ void epi_store(const TcProblem& P, const TileCoord& tc,
                                           float (&acc)[BN / 2], int warp, int lane,
                                           float* stage_base) {
-  using S = TcShape<NP, BN, (split_stage_k(NP) > kTcKB)>;
+  using S = TcShape<NP, BN, false>;  // only its BN-dependent staging is read here
   constexpr int HALF = BN / 2;
   const int ew = warp - 2;
   const int q = warp & 3;
@@ -327,7 +326,7 @@ __device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
                                                uint64_t* main_empty, uint64_t* tile_full,
                                                uint64_t* tmem_empty, int chunk_kb, int fmt,
                                                int* err) {
-  constexpr bool WIDE = split_stage_k(NP) > kTcKB;
+  constexpr bool WIDE = tc_wide(NP, TF32);
   using S = TcShape<NP, BN, WIDE>;
   constexpr int KK = S::KB / 16;  // k steps of 32 bytes per row in a stage
   constexpr uint32_t SBO = WIDE ? 1024 : 512, SWZ = WIDE ? 2 : 4;
@@ -428,7 +427,7 @@ __global__ void __launch_bounds__(FUSED ? fused_threads(BN) : kTcThreads, 1)
   static_assert(!FUSED || (NP == 3 && GROUPED && !TF32), "fused: grouped bf16x3-piece launches");
   // 256-wide fused tiles: the epilogue warps are the converters
   constexpr bool DUAL = FUSED && BN == 256;
-  constexpr bool WIDE = split_stage_k(NP) > kTcKB;
+  constexpr bool WIDE = tc_wide(NP, TF32);
   using S = TcShape<NP, BN, WIDE>;
   constexpr int KB = S::KB;
   // K-major operand tiles: 8-row groups of 128-byte rows (128-byte swizzle)
@@ -1540,7 +1539,7 @@ ugemm_status launch_kernel(const CUtensorMap& ta, const CUtensorMap& tb, const T
                            const CUtensorMap* maps, const TcProblem* probs, const int4* tiles,
                            int total_tiles, int nprod, int chunk_kb, int max_ctas, int fmt,
                            int* dev_err, cudaStream_t st) {
-  using S = TcShape<NP, BN, (split_stage_k(NP) > kTcKB)>;
+  using S = TcShape<NP, BN, tc_wide(NP, TF32)>;
   auto kern = split_tc_kernel<NP, BN, GROUPED, EPI, TF32, FUSED>;
   static std::atomic<uint64_t> attr_done{0};  // per instantiation and device
   constexpr size_t kSmem = FUSED ? S::SMEM_FUSED : S::SMEM;
@@ -1649,8 +1648,8 @@ size_t split_scratch_bytes(const Gemm& g, const SplitPlan& p) {
          tail_scratch_bytes(g, p);
 }
 
-// Boxes of one stage: split_stage_k(pieces) deep, 128-byte swizzle for
-// 64-deep stages, 64-byte swizzle for 32-deep ones.
+// Boxes of one stage: split_stage_k(pieces) deep, the swizzle as wide as a
+// row of the box (128 bytes for TF32 pieces, 64 for 16-bit ones).
 CUtensorMapSwizzle split_swizzle(int pieces) {
   return split_stage_k(pieces) * piece_bytes(pieces) == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
                                                             : CU_TENSOR_MAP_SWIZZLE_64B;

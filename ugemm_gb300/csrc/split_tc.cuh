@@ -93,11 +93,8 @@ __host__ __device__ __forceinline__ void tc_raster(int local, int tiles_m, int t
   n0 = ((local % per_group) / group_rows) * block_n;
 }
 
-// WIDE: 64-deep stages of 128-byte rows (128-byte swizzle) instead of
-// 32-deep ones of 64-byte rows.  Each stage carries a fixed cost on top of
-// its MMAs (measured: ~0.26 us per stage whatever its MMA count), so the
-// two-piece forms, with few MMAs per k, take two k-blocks per stage; their
-// stage (96 KB at BN = 256) leaves room for two (split_stage_k).
+// WIDE: stages of 128-byte rows (128-byte swizzle; 64 16-bit elements deep,
+// the TF32 form's 32 tf32 elements) instead of 64-byte ones.
 template <int NP, int BN, bool WIDE = false>
 struct TcShape {
   static constexpr int KB = WIDE ? 2 * kTcKB : kTcKB;  // k depth of a stage
@@ -203,11 +200,18 @@ constexpr int piece_bytes(int code) { return code == kPiecesTf32 ? 4 : 2; }
 // The GEMM kernel instantiation a layout runs on: TF32 stages have the
 // shape of the two-piece 16-bit ones (two planes of 128-byte rows).
 constexpr int kernel_np(int code) { return code == kPiecesTf32 ? 2 : code; }
-// k depth of one pipeline stage: 64 for two 16-bit pieces and 32 for TF32
-// pieces (128-byte rows, 128-byte swizzle), 32 for three 16-bit pieces
-// (64-byte rows, 64-byte swizzle).  The tensor maps' boxes and every
-// launch's TcProblem::nkb follow it.
-constexpr int split_stage_k(int code) { return code == 2 ? 2 * kTcKB : kTcKB; }
+// k depth of one pipeline stage: 32 elements in every layout -- 64-byte
+// rows with the 64-byte swizzle for 16-bit pieces, 128-byte rows with the
+// 128-byte swizzle for TF32 pieces.  The tensor maps' boxes and every
+// launch's TcProblem::nkb follow it.  (Two-piece 16-bit operands once took
+// 64-deep stages of 128-byte rows, two 96 KB stages at 256-wide tiles, to
+// halve a per-stage cost of the MMA issuer; with that cost gone, 32-deep
+// stages in a four-stage ring are faster: FP16x3 GEMM at 8192^3 1.93 ->
+// 1.88 ms.)
+constexpr int split_stage_k(int /*code*/) { return kTcKB; }
+// Whether a kernel instantiation has the 128-byte-row shape (TcShape WIDE):
+// the TF32 form's stages, on the two-piece instantiation.
+constexpr bool tc_wide(int np, bool tf32) { return np == 2 && tf32; }
 // Stages of the kernel's depth over K, and a chunk of `chunk_kb` 32-deep
 // k-blocks in stages.
 inline int split_nkb(int pieces, int K) {
