@@ -359,13 +359,10 @@ __device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
     // the epilogue must have read this buffer's previous tile
     if (use > 0 && !mbar_wait(&tmem_empty[buf], (use - 1) & 1, err, kDevTimeoutAccum)) return;
     tc_fence_after();
-    int cpos = 0;  // the k-block's position in its chunk
-    for (int kb = 0; kb < P.nkb; ++kb) {
-      if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) return;
-      tc_fence_after();
-      const uint64_t so = (s * static_cast<uint32_t>(S::STAGE_BYTES)) >> 4;
+    // the descriptors of stage st; the MMAs of its corrections and main product
+    auto corrections = [&](uint32_t st, int kbi) {
+      const uint64_t so = (st * static_cast<uint32_t>(S::STAGE_BYTES)) >> 4;
       const uint64_t da = da0 + so, db = db0 + so;
-      // correction products into their own accumulator
 #pragma unroll
       for (int p = 0; p < NPROD - 1; ++p) {
         const uint32_t ia = corr_code(p) >> 2, ib = corr_code(p) & 3;
@@ -373,31 +370,63 @@ __device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
         for (int kk = 0; kk < KK; ++kk) {
           const uint64_t a = da + ((ia * S::A_PLANE + kk * 32) >> 4);
           const uint64_t b = db + ((ib * S::B_PLANE + kk * 32) >> 4);
-          if constexpr (TF32) umma_tf32(t_corr, a, b, idesc, (kb | p | kk) != 0);
-          else umma_bf16(t_corr, a, b, idesc, (kb | p | kk) != 0);
+          if constexpr (TF32) umma_tf32(t_corr, a, b, idesc, (kbi | p | kk) != 0);
+          else umma_bf16(t_corr, a, b, idesc, (kbi | p | kk) != 0);
         }
       }
-      // main product; a new chunk restarts the accumulator once drained
-      const bool chunk_start = cpos == 0;
-      if (chunk_start && kb > 0) {
+    };
+    auto main_product = [&](uint32_t st, bool restart) {
+      const uint64_t so = (st * static_cast<uint32_t>(S::STAGE_BYTES)) >> 4;
+      const uint64_t da = da0 + so, db = db0 + so;
+#pragma unroll
+      for (int kk = 0; kk < KK; ++kk) {
+        const uint64_t a = da + ((kk * 32) >> 4), b = db + ((kk * 32) >> 4);
+        if constexpr (TF32) umma_tf32(t_main, a, b, idesc, !(restart && kk == 0));
+        else umma_bf16(t_main, a, b, idesc, !(restart && kk == 0));
+      }
+    };
+    int cpos = 0;  // the k-block's position in its chunk
+    for (int kb = 0; kb < P.nkb;) {
+      if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) return;
+      tc_fence_after();
+      corrections(s, kb);
+      // A new chunk restarts the main accumulator once the epilogue has
+      // drained the last one.  While that drain runs, the corrections of the
+      // next stages already in shared memory (the rest of the ring, within
+      // this chunk) go ahead, so the tensor pipe does not wait; each
+      // accumulator still receives its products in stage order (the same
+      // bits).  Without this, every chunk start cost ~850 cycles of idle
+      // tensor pipe in the three-product form.
+      int ahead = 0;
+      if (cpos == 0 && kb > 0) {
+        uint32_t s2 = s + 1 == NST ? 0 : s + 1, ph2 = s + 1 == NST ? ph ^ 1 : ph;
+        while (ahead < NST - 1 && ahead + 1 < chunk_kb && kb + 1 + ahead < P.nkb &&
+               !mbar_test_wait(&main_empty[buf], nbound[buf] & 1) && mbar_test_wait(&full[s2], ph2)) {
+          tc_fence_after();
+          corrections(s2, kb + 1 + ahead);
+          ++ahead;
+          if (++s2 == NST) {
+            s2 = 0;
+            ph2 ^= 1;
+          }
+        }
         if (!mbar_wait(&main_empty[buf], nbound[buf] & 1, err, kDevTimeoutAccum)) return;
         ++nbound[buf];
         tc_fence_after();
       }
-#pragma unroll
-      for (int kk = 0; kk < KK; ++kk) {
-        const uint64_t a = da + ((kk * 32) >> 4), b = db + ((kk * 32) >> 4);
-        if constexpr (TF32) umma_tf32(t_main, a, b, idesc, !(chunk_start && kk == 0));
-        else umma_bf16(t_main, a, b, idesc, !(chunk_start && kk == 0));
-      }
-      umma_commit(&empty[s]);
-      if (++cpos == chunk_kb) {
-        cpos = 0;
-        if (kb + 1 < P.nkb) umma_commit(&main_full[buf]);
-      }
-      if (++s == NST) {
-        s = 0;
-        ph ^= 1;
+      // the main products of this stage and of those whose corrections went
+      // ahead, each stage released once its MMAs complete
+      for (int a = 0; a <= ahead; ++a, ++kb) {
+        main_product(s, cpos == 0);
+        umma_commit(&empty[s]);
+        if (++cpos == chunk_kb) {
+          cpos = 0;
+          if (kb + 1 < P.nkb) umma_commit(&main_full[buf]);
+        }
+        if (++s == NST) {
+          s = 0;
+          ph ^= 1;
+        }
       }
     }
     umma_commit(&tile_full[buf]);
