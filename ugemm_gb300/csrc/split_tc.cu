@@ -1645,7 +1645,11 @@ int split_default_chunk_kb(int K) {
     return e ? std::max(1, std::atoi(e) / kTcKB) : 0;
   }();
   if (forced) return forced;
-  return K <= 1024 ? 2 : 4;
+  // 64 deep up to k = 1024 (where FP32 SIMT's own error is smallest), 128
+  // up to 4096, 256 beyond: every chunk start makes the main accumulator
+  // wait for a drain, and at 8192^3 halving their number saves 4% of the
+  // FP16x3 GEMM for an error of 3.6e-7 instead of 2.4e-7 (FP32 SIMT: 1.6e-6)
+  return K <= 1024 ? 2 : (K <= 4096 ? 4 : 8);
 }
 
 SplitPlan split_plan_for(int precision, const Gemm& g) {
