@@ -677,11 +677,11 @@ __global__ void __launch_bounds__(FUSED ? fused_threads(BN) : kTcThreads, 1)
 template <int NP, int FMT>
 __device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t (&out)[NP]) {
   if constexpr (FMT == 1) {
+    // paired conversions (each element rounded to nearest, as single ones)
     const float y0 = scale_pow2(x0, e), y1 = scale_pow2(x1, e);
-    const __half h00 = __float2half_rn(y0), h01 = __float2half_rn(y1);
-    const __half2 hi = __halves2half2(h00, h01);
-    const __half2 lo = __halves2half2(__float2half_rn(y0 - __half2float(h00)),
-                                      __float2half_rn(y1 - __half2float(h01)));
+    const __half2 hi = __float22half2_rn(make_float2(y0, y1));
+    const float2 back = __half22float2(hi);
+    const __half2 lo = __float22half2_rn(make_float2(y0 - back.x, y1 - back.y));
     out[0] = *reinterpret_cast<const uint32_t*>(&hi);
     out[1] = *reinterpret_cast<const uint32_t*>(&lo);
     return;
