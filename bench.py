@@ -551,6 +551,9 @@ def main():
     peak_split = pk["bf16_tflops"] / split_forms[head]
     sm_max = pk.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    # the FP32 FMA rate measured on this GPU (no FP32 figure is in the
+    # measured-peaks file): 200 ms of independent FMA chains
+    fp32_measured = ug.fp32_peak(200.0)
     traffic = None  # DRAM bytes of the GEMM phase from the committed ncu capture (8192^3)
     try:
         with open(os.path.join(ROOT, "profiles", "split_tc_kernel_sgemm8192_traffic.json")) as f:
@@ -586,6 +589,8 @@ def main():
                           "worst_row_err_fp64": errs_main["simt"][1],
                           "wide40_4096_err_fp64": dict(zip(("normwise", "worst_row", "worst_col"),
                                                            errs_wide["simt"])),
+                          "frac_of_fp32_peak_measured": round(tflops_simt / fp32_measured, 4),
+                          "fp32_peak_measured_tflops": round(fp32_measured, 2),
                           "frac_of_fp32_peak_nominal": round(tflops_simt / fp32_peak, 4),
                           "fp32_peak_nominal_tflops": round(fp32_peak, 2)},
             "split_over_simt": round(tflops_split / tflops_simt, 3),

@@ -370,6 +370,12 @@ UGEMM_API int ugemm_sgemv(char trans, int M, int N, float alpha, const float *A,
 UGEMM_API int ugemm_profile_enable(int on);
 UGEMM_API int ugemm_profile_collect(double *ms_per_kind, int *launches_per_kind, int nkinds);
 
+/* Measured FP32 FMA peak of the current device in TFLOP/s (no reference
+ * counterpart; measurement infrastructure: the roofline of the plain SIMT
+ * form).  Runs eight independent FMA chains per thread, 32 warps per SM, for
+ * about `ms` milliseconds after a warm-up launch, timed with CUDA events. */
+UGEMM_API int ugemm_fp32_peak(double ms, double *tflops);
+
 /* Failure-detection self-test (no reference counterpart; the reference's
  * OpenCL calls have no device-side failure detection).  Runs one small
  * kernel whose threads wait, through the library's bounded mbarrier wait with

@@ -257,3 +257,13 @@ def test_deep_narrow_gemm_runs_split_k(ta, tb, beta):
     err = float(torch.linalg.norm(C[:, :N].double() - ref) / torch.linalg.norm(ref))
     assert err < 2e-6, err
     assert torch.equal(C[:, N:], C0[:, N:])
+
+
+def test_fp32_peak_probe_is_a_plausible_rate():
+    """The measured FP32 FMA peak the benchmark divides the SIMT form by:
+    positive, below the nominal rate of 128 FMA lanes per SM at the
+    device's maximum clock, and above half of it."""
+    props = torch.cuda.get_device_properties(0)
+    nominal = props.multi_processor_count * 128 * 2 * 2.07e9 / 1e12
+    peak = ug.fp32_peak(50.0)
+    assert 0.5 * nominal < peak < 1.05 * nominal, (peak, nominal)

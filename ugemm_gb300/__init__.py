@@ -318,6 +318,15 @@ def device_info():
     return sm.value, ma.value, mi.value
 
 
+def fp32_peak(ms: float = 200.0) -> float:
+    """Measured FP32 FMA peak of the current device, TFLOP/s."""
+    lib = load()
+    lib.ugemm_fp32_peak.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    out = ctypes.c_double()
+    _check(lib.ugemm_fp32_peak(ms, ctypes.byref(out)))
+    return out.value
+
+
 def profile_enable(on: bool = True) -> None:
     _check(load().ugemm_profile_enable(1 if on else 0))
 
