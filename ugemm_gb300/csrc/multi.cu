@@ -222,8 +222,10 @@ ugemm_status tail_launch(const Gemm& g, const SplitPlan& p, const TailPlan& tail
   if (epi.bias) epi.bias += tail.r0;
   t.red[0] = ReduceJob{part, g.C + size_t(tail.r0) * g.ldc + tail.c0, Mt, Nt, g.ldc, 2, g.beta, epi};
   const int grid = std::max(1, std::min(tiles, sm_count()));
+  prof_begin(st);
   multi_table_kernel<<<std::max(1, std::min(cdiv(tiles, 256), 64)), 256, 0, st>>>(
       t, 2, tiles, p.block_n, grid, reinterpret_cast<MultiTable*>(tab), recs);
+  prof_end(st, kProfControl);
   if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
   SplitPlan q = p;
   q.epi = false;
@@ -324,8 +326,10 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
   }
   uint8_t* tab = base + L.table_off;
   int4* recs = reinterpret_cast<int4*>(base + L.recs_off);
+  prof_begin(st);
   multi_table_kernel<<<std::max(1, std::min(cdiv(tiles, 256), 64)), 256, 0, st>>>(
       t, nsub, tiles, p.block_n, L.grid, reinterpret_cast<MultiTable*>(tab), recs);
+  prof_end(st, kProfControl);
   if (cudaPeekAtLastError() != cudaSuccess) return UGEMM_ERR_CUDA;
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
