@@ -514,9 +514,12 @@ __global__ void __launch_bounds__(FUSED ? fused_threads(BN) : kTcThreads, 1)
 
   if (FUSED && !DUAL && warp >= 2 + kTcEpiWarps) {
     // ------------------------------------------------- fused converters
+    // threads of warps 12 and 13 first (see fused_convert)
+    static_assert(kTcConvWarps == 6 && 2 + kTcEpiWarps == 10, "converter warps 10-15");
     if constexpr (FUSED && !DUAL)
       fused_convert<NP, BN>(probs, tiles, smem, smem + NST * S::STAGE_BYTES, full, empty,
-                            raw_full, raw_empty, (warp - 2 - kTcEpiWarps) * 32 + lane, err);
+                            raw_full, raw_empty, ((warp - 2 - kTcEpiWarps + 4) % 6) * 32 + lane,
+                            err);
   } else if (FUSED && warp == 0) {
     // ------------------------------------------- fused raw TMA producer
     if (lane == 0) {
@@ -670,6 +673,30 @@ __global__ void __launch_bounds__(FUSED ? fused_threads(BN) : kTcThreads, 1)
 }
 
 // ---------------------------------------------------------------- split pass
+// r - p for a packed pair p of 16-bit pieces (x in the low half, y in the
+// high half) as two mixed-precision FMAs, p * -1 + r, that read the 16-bit
+// halves directly: no widening of the pieces to FP32 first.  The difference
+// is exact in FP32 (p is r rounded to 8 or 11 significant bits), so this is
+// the same value as the subtraction after widening.  The split is bound by
+// the integer/conversion pipe in the fused converters; the FMAs run on the
+// FP32 pipe (fused 256-problem group: 164 -> 151 us).
+__device__ __forceinline__ float2 sub_pieces_bf16x2(uint32_t p, float2 r) {
+  float2 d;
+  asm("{\n\t.reg .b16 lo, hi, m1;\n\tmov.b32 {lo, hi}, %2;\n\tmov.b16 m1, 0xBF80;\n\t"
+      "fma.rn.f32.bf16 %0, lo, m1, %3;\n\tfma.rn.f32.bf16 %1, hi, m1, %4;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "r"(p), "f"(r.x), "f"(r.y));
+  return d;
+}
+__device__ __forceinline__ float2 sub_pieces_f16x2(uint32_t p, float2 r) {
+  float2 d;
+  asm("{\n\t.reg .b16 lo, hi, m1;\n\tmov.b32 {lo, hi}, %2;\n\tmov.b16 m1, 0xBC00;\n\t"
+      "fma.rn.f32.f16 %0, lo, m1, %3;\n\tfma.rn.f32.f16 %1, hi, m1, %4;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "r"(p), "f"(r.x), "f"(r.y));
+  return d;
+}
+
 // Pieces of two consecutive k of one row, each piece plane as one packed
 // 16-bit pair: bf16 pieces (FMT 0: x0 = bf16(x), x1 = bf16(x - x0), ...) or
 // the FP16x3 form's two fp16 pieces of x * 2^e (FMT 1; e = the row's
@@ -680,9 +707,8 @@ __device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t 
     // paired conversions (each element rounded to nearest, as single ones)
     const float y0 = scale_pow2(x0, e), y1 = scale_pow2(x1, e);
     const __half2 hi = __float22half2_rn(make_float2(y0, y1));
-    const float2 back = __half22float2(hi);
-    const __half2 lo = __float22half2_rn(make_float2(y0 - back.x, y1 - back.y));
     out[0] = *reinterpret_cast<const uint32_t*>(&hi);
+    const __half2 lo = __float22half2_rn(sub_pieces_f16x2(out[0], make_float2(y0, y1)));
     out[1] = *reinterpret_cast<const uint32_t*>(&lo);
     return;
   }
@@ -702,11 +728,7 @@ __device__ __forceinline__ void pieces_pair(float x0, float x1, int e, uint32_t 
     }
     const __nv_bfloat162 two = __float22bfloat162_rn(rem);
     out[p] = *reinterpret_cast<const uint32_t*>(&two);
-    if (p + 1 < NP) {
-      const float2 back = __bfloat1622float2(two);
-      rem.x -= back.x;
-      rem.y -= back.y;
-    }
+    if (p + 1 < NP) rem = sub_pieces_bf16x2(out[p], rem);
   }
 }
 
@@ -1166,6 +1188,13 @@ __global__ void __launch_bounds__(256) operand_max_batched_kernel(const SplitJob
 // full barrier and the raw stage's empty barrier.  (Loading a stage's
 // chunks two at a time between stores left each load's latency exposed:
 // 13% slower at 4096^3.)
+//
+// The split is bound by the integer/conversion pipe, so the chunks' raw and
+// piece offsets are computed once per tile, not per stage (256-problem
+// group: 150 -> 140 us).  The converter warps are warps 10-15 of the CTA, on
+// SM sub-partitions 2, 3, 0, 1, 2, 3: the caller numbers the threads of
+// warps 12 and 13, alone on theirs, first, so that the chunks left over
+// after five rounds (threads 0-63 take a sixth) fall to them (140 -> 137 us).
 template <int NP, int BN>
 __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* __restrict__ tiles,
                               uint8_t* pieces, uint8_t* raw, uint64_t* full, uint64_t* empty,
@@ -1178,12 +1207,31 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
                 "a warp's chunks are all of one operand");
   static_assert(kTcKB == 32 && S::RAW_K == kTcKB,
                 "32-deep stages: 128-byte raw rows, 64-byte piece rows");
+  static_assert(S::RAW_A % 32 == 0, "bit 4 of a raw offset is bit 0 of its 16-byte unit");
   const int4 range = tiles[blockIdx.x];
   uint32_t it = 0;
   for (int t = range.x; t < range.y; ++t) {
     const int4 rec = tiles[gridDim.x + t];
     const TcProblem& P = probs[rec.x];
     const int nkb = P.nkb, kc_a = P.kc_a, kc_b = P.kc_b;
+    // this tile's chunk offsets: raw bytes from the raw stage (for a
+    // [rows][32] tile the first of its two units; the second is at bit 4
+    // flipped: unit (2c + 1) ^ (r & 7) = ((2c) ^ (r & 7)) ^ 1) and piece bytes
+    // from the piece stage
+    uint32_t ldo[PER], sto[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int ch = ct + kTcConvThreads * i;
+      const bool is_a = ch < CH_A;
+      const int local = is_a ? ch : ch - CH_A, nrows = is_a ? kTcBM : BN;
+      const bool kc = is_a ? kc_a : kc_b;
+      const int r = kc ? local >> 2 : local % nrows, c = kc ? local & 3 : local / nrows;
+      ldo[i] = (is_a ? 0u : uint32_t(S::RAW_A)) +
+               (kc ? uint32_t(r * 128 + (((2 * c) ^ (r & 7)) << 4))
+                   : uint32_t(((8 * c) * nrows + r) * 4));
+      sto[i] = (is_a ? 0u : uint32_t(S::A_BYTES)) + static_cast<uint32_t>(r) * 64 +
+               ((c ^ ((r >> 1) & 3)) << 4);
+    }
     for (int kb = 0; kb < nkb; ++kb, ++it) {
       const int rs = it % kTcRawStages, ps = it % kTcFusedPieceStages;
       if (!__all_sync(0xffffffffu,
@@ -1196,18 +1244,14 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
         const int ch = ct + kTcConvThreads * i;
         if (CH % kTcConvThreads != 0 && ch >= CH) continue;
         const bool is_a = ch < CH_A;
-        const int local = is_a ? ch : ch - CH_A, nrows = is_a ? kTcBM : BN;
-        const uint8_t* src = is_a ? ra : ra + S::RAW_A;
         if (is_a ? kc_a : kc_b) {  // [rows][32] floats, 128-byte swizzle
-          const int r = local >> 2, c = local & 3;
-          const uint8_t* row = src + r * 128;
-          const float4 lo = *reinterpret_cast<const float4*>(row + (((2 * c) ^ (r & 7)) << 4));
-          const float4 hi = *reinterpret_cast<const float4*>(row + (((2 * c + 1) ^ (r & 7)) << 4));
+          const float4 lo = *reinterpret_cast<const float4*>(ra + ldo[i]);
+          const float4 hi = *reinterpret_cast<const float4*>(ra + (ldo[i] ^ 16u));
           v[i][0] = lo.x; v[i][1] = lo.y; v[i][2] = lo.z; v[i][3] = lo.w;
           v[i][4] = hi.x; v[i][5] = hi.y; v[i][6] = hi.z; v[i][7] = hi.w;
         } else {  // [32][rows] floats
-          const int r = local % nrows, c = local / nrows;
-          const float* col = reinterpret_cast<const float*>(src) + (8 * c) * nrows + r;
+          const int nrows = is_a ? kTcBM : BN;
+          const float* col = reinterpret_cast<const float*>(ra + ldo[i]);
 #pragma unroll
           for (int e = 0; e < 8; ++e) v[i][e] = col[e * nrows];
         }
@@ -1220,10 +1264,7 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
       for (int i = 0; i < PER; ++i) {
         const int ch = ct + kTcConvThreads * i;
         if (CH % kTcConvThreads != 0 && ch >= CH) continue;
-        const bool is_a = ch < CH_A;
-        const int local = is_a ? ch : ch - CH_A, nrows = is_a ? kTcBM : BN;
-        const bool kc = is_a ? kc_a : kc_b;
-        const int r = kc ? local >> 2 : local % nrows, c = kc ? local & 3 : local / nrows;
+        const int plane = ch < CH_A ? S::A_PLANE : S::B_PLANE;
         uint32_t packed[NP][4];
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
@@ -1232,12 +1273,9 @@ __device__ void fused_convert(const TcProblem* __restrict__ probs, const int4* _
 #pragma unroll
           for (int p = 0; p < NP; ++p) packed[p][e / 2] = two[p];
         }
-        uint8_t* base = is_a ? pa : pa + S::A_BYTES;
-        const int plane = is_a ? S::A_PLANE : S::B_PLANE;
-        const uint32_t off = static_cast<uint32_t>(r) * 64 + ((c ^ ((r >> 1) & 3)) << 4);
 #pragma unroll
         for (int p = 0; p < NP; ++p)
-          *reinterpret_cast<uint4*>(base + p * plane + off) =
+          *reinterpret_cast<uint4*>(pa + sto[i] + p * plane) =
               make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
       }
       // the stores and the raw loads, ordered before the tensor core reads
