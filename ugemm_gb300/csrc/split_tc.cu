@@ -887,9 +887,26 @@ __device__ __forceinline__ void load_raw(const SplitJob& j, int r0, int k0, RawT
         pix = r0 + q4;
         n = tap < j.K ? j.rows - pix : 0;
       }
-      // walk the image row: one address per row, a step of `stride` per pixel
       const Im2colTap tp = im2col_tap(j.im, tap);
       Im2colPix px = im2col_pix(j.im, pix);
+      if ((j.im.Wo & 3) == 0) {
+        // pix is a multiple of 4, so the 4 pixels lie in one image row (and
+        // all exist when the first does): one row address, one bounds test
+        // per pixel, no walk
+        const int yy = px.i * j.im.stride - j.im.pad + tp.ki;
+        const int x0 = px.j * j.im.stride - j.im.pad + tp.kj;
+        const bool ok = n > 0 && static_cast<unsigned>(yy) < static_cast<unsigned>(j.im.H);
+        const float* row = j.im.x + ((static_cast<long long>(tp.c) * j.im.B + px.b) * j.im.H +
+                                     (ok ? yy : 0)) * static_cast<long long>(j.im.W);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int xx = x0 + e * j.im.stride;
+          out.v[i][e] =
+              (ok && static_cast<unsigned>(xx) < static_cast<unsigned>(j.im.W)) ? row[xx] : 0.f;
+        }
+        continue;
+      }
+      // walk the image row: one address per row, a step of `stride` per pixel
       int xx = px.j * j.im.stride - j.im.pad + tp.kj;
       int yy = px.i * j.im.stride - j.im.pad + tp.ki;
       const float* row = j.im.x + ((static_cast<long long>(tp.c) * j.im.B + px.b) * j.im.H + yy) *
