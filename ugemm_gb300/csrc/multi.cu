@@ -268,6 +268,9 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
 
   MultiTable t;
   std::memset(&t, 0, sizeof t);
+  SplitJobTable jt{};
+  static_assert(2 * kMultiMax <= kSplitTableJobs, "two operands per GEMM");
+  int nj = 0, split_tiles = 0;
   int nsub = 0, nred = 0, tiles = 0;
   long long red_max = 0;
   for (int i = 0; i < n; ++i) {
@@ -277,9 +280,19 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
     void* bp = base + L.b_off[i];
     long long a_sr, a_sk, b_sr, b_sk;
     split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
-    ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st, p.f16);
-    if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st, p.f16);
-    if (s != UGEMM_OK) return s;
+    if (p.f16) {  // the FP16x3 split needs each operand's row maxima first
+      ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st, true);
+      if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st, true);
+      if (s != UGEMM_OK) return s;
+    } else {  // every operand in one split launch (below)
+      const int kp = split_kp(g.K), tk = cdiv(kp, 64);
+      jt.jobs[nj++] = SplitJob{g.A, a_sr, a_sk, static_cast<__nv_bfloat16*>(ap), g.M, g.K, kp,
+                               split_tiles};
+      split_tiles += cdiv(g.M, 32) * tk;
+      jt.jobs[nj++] = SplitJob{g.B, b_sr, b_sk, static_cast<__nv_bfloat16*>(bp), g.N, g.K, kp,
+                               split_tiles};
+      split_tiles += cdiv(g.N, 32) * tk;
+    }
     const bool ok = o.swap ? split_encode_maps(p.pieces, p.block_n, bp, g.N, ap, g.M, g.K,
                                                &t.maps[2 * i], &t.maps[2 * i + 1])
                            : split_encode_maps(p.pieces, p.block_n, ap, g.M, bp, g.N, g.K,
@@ -323,6 +336,12 @@ ugemm_status multi_launch(const Gemm* gs, int n, const SplitPlan& plan, Scratch 
   for (int j = 0; j < nsub; ++j) {
     t.probs[j].tile_start = tiles;
     tiles += t.probs[j].tiles_m * t.probs[j].tiles_n;
+  }
+  // the operands' bf16 / TF32 pieces: one launch for all of them (four
+  // launches of one operand each left a ramp and a tail apiece)
+  if (nj > 0) {
+    const ugemm_status s = split_param_launch(p.pieces, jt, nj, split_tiles, st);
+    if (s != UGEMM_OK) return s;
   }
   uint8_t* tab = base + L.table_off;
   int4* recs = reinterpret_cast<int4*>(base + L.recs_off);

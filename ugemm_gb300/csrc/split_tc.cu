@@ -1015,8 +1015,8 @@ __device__ __forceinline__ void tile_origin(const SplitJob& j, int b, int& r0, i
 }
 
 template <int NP, int FMT>
-__global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
-                                                                   int njobs, int total_tiles) {
+__device__ __forceinline__ void split_batched_body(const SplitJob* __restrict__ jobs, int njobs,
+                                                   int total_tiles) {
   __shared__ float tile[32][65];
   __shared__ int starts[kJobCache];
   const int cached = min(njobs, kJobCache);
@@ -1046,6 +1046,21 @@ __global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJo
     r0 = nr0;
     k0 = nk0;
   }
+}
+
+template <int NP, int FMT>
+__global__ void __launch_bounds__(256) split_pieces_batched_kernel(const SplitJob* __restrict__ jobs,
+                                                                   int njobs, int total_tiles) {
+  split_batched_body<NP, FMT>(jobs, njobs, total_tiles);
+}
+
+// The same for a few operands whose job records travel as the kernel's
+// parameter (read through the constant cache): nothing to write to device
+// memory first, so a sequence of launches stays capture-safe without a table.
+template <int NP, int FMT>
+__global__ void __launch_bounds__(256) split_pieces_param_kernel(
+    const __grid_constant__ SplitJobTable t, int njobs, int total_tiles) {
+  split_batched_body<NP, FMT>(t.jobs, njobs, total_tiles);
 }
 
 // FP16x3 form, first step of the split: the largest finite magnitude of
@@ -1870,6 +1885,20 @@ ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, i
   if (pieces == 3) split_pieces_batched_kernel<3, 0><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
   else if (pieces == kPiecesTf32) split_pieces_batched_kernel<2, 2><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
   else split_pieces_batched_kernel<2, 0><<<grid, 256, 0, st>>>(jobs, njobs, total_tiles);
+  prof_end(st, kProfSplitPrep);
+  return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+}
+
+ugemm_status split_param_launch(int pieces, const SplitJobTable& t, int njobs, int total_tiles,
+                                cudaStream_t st) {
+  if (total_tiles <= 0) return UGEMM_OK;
+  if (njobs < 1 || njobs > kSplitTableJobs) return UGEMM_ERR_ARG;
+  const int grid = std::min(total_tiles, sm_count() * 8);
+  prof_begin(st);
+  if (pieces == 3) split_pieces_param_kernel<3, 0><<<grid, 256, 0, st>>>(t, njobs, total_tiles);
+  else if (pieces == kPiecesTf32) split_pieces_param_kernel<2, 2><<<grid, 256, 0, st>>>(t, njobs, total_tiles);
+  else if (pieces == 2) split_pieces_param_kernel<2, 0><<<grid, 256, 0, st>>>(t, njobs, total_tiles);
+  else { prof_end(st, kProfSplitPrep); return UGEMM_ERR_ARG; }
   prof_end(st, kProfSplitPrep);
   return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
 }

@@ -267,6 +267,15 @@ std::vector<int4> split_tile_table(const TcProblem* probs, int nprob, int block_
 // The batched pre-pass of a grouped plan.  fmax_words (FP16x3 plans): the
 // jobs' `fmax` row words, nwords of them contiguous, cleared and filled
 // before the split.
+// A few split jobs passed by value (split_param_launch): tile_start of each
+// job is its first 32 x 64 tile in the launch.  bf16 and TF32 pieces only
+// (the FP16x3 form's row maxima take their own passes).
+constexpr int kSplitTableJobs = 8;
+struct SplitJobTable {
+  SplitJob jobs[kSplitTableJobs];
+};
+ugemm_status split_param_launch(int pieces, const SplitJobTable& t, int njobs, int total_tiles,
+                                cudaStream_t st);
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
                                   cudaStream_t st, unsigned* fmax_words = nullptr, int nwords = 0);
 // Split one operand into its pieces at dst (split_operand_bytes of room).
