@@ -1175,6 +1175,56 @@ __global__ void __launch_bounds__(256) operand_row_max_kernel(const float* __res
   }
 }
 
+// FP16x3 split of an operand whose rows are contiguous in k (sk == 1), 16-byte
+// aligned, with K <= kRowSplitK: one block per row keeps the whole row in
+// registers (32 values a thread), takes its largest finite magnitude, writes
+// the row's word and splits the registers -- one read of the operand instead
+// of a row-maximum pass and a split pass that reads it again.  Same word,
+// same scale and same pieces as the two passes.
+constexpr int kRowSplitK = 8192;
+__global__ void __launch_bounds__(256) split_rows_f16_kernel(const float* __restrict__ src,
+                                                             long long sr, int K, int Kp,
+                                                             __nv_bfloat16* __restrict__ dst,
+                                                             int rows, unsigned* words) {
+  constexpr int CH = kRowSplitK / (256 * 8);  // 8-k chunks a thread
+  __shared__ float part[8];
+  const int t = threadIdx.x, r = blockIdx.x;
+  const float* row = src + r * sr;
+  float v[CH][8];
+  float m = 0.f;
+#pragma unroll
+  for (int j = 0; j < CH; ++j) {
+    const int k0 = 2048 * j + 8 * t;
+    if (k0 + 7 < K) {
+      const float4 lo = *reinterpret_cast<const float4*>(row + k0);
+      const float4 hi = *reinterpret_cast<const float4*>(row + k0 + 4);
+      v[j][0] = lo.x; v[j][1] = lo.y; v[j][2] = lo.z; v[j][3] = lo.w;
+      v[j][4] = hi.x; v[j][5] = hi.y; v[j][6] = hi.z; v[j][7] = hi.w;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) v[j][e] = k0 + e < K ? row[k0 + e] : 0.f;
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) m = fmaxf(m, finite_abs(v[j][e]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((t & 31) == 0) part[t >> 5] = m;
+  __syncthreads();
+  m = part[0];
+#pragma unroll
+  for (int w = 1; w < 8; ++w) m = fmaxf(m, part[w]);
+  const unsigned bits = __float_as_uint(m);
+  if (t == 0) words[r] = bits;
+  const int ex = f16_scale_exp(bits);
+  const size_t plane = static_cast<size_t>(rows) * Kp;
+#pragma unroll
+  for (int j = 0; j < CH; ++j) {
+    const int k0 = 2048 * j + 8 * t;
+    if (k0 < Kp) store_pieces8<2, 1>(dst, plane, static_cast<size_t>(r) * Kp + k0, v[j], ex);
+  }
+}
+
 // One operand of any strides through the tiled reduction, tiles grid-stride.
 __global__ void __launch_bounds__(256) operand_max_single_kernel(const __grid_constant__ SplitJob j,
                                                                  int total_tiles) {
@@ -1816,8 +1866,19 @@ ugemm_status split_launch(const Gemm& g, const SplitPlan& p, Scratch ws, int* de
   uint8_t* tail_scratch = bp + split_operand_bytes(p.pieces, g.N, g.K);
   long long a_sr, a_sk, b_sr, b_sk;
   split_operand_strides(g, &a_sr, &a_sk, &b_sr, &b_sk);
-  ugemm_status s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st, p.f16);
-  if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st, p.f16);
+  ugemm_status s = UGEMM_OK;
+  if (!p.f16 && g.M > 0 && g.N > 0 && g.K > 0) {
+    // both operands in one launch (the FP16x3 split takes row-maximum
+    // passes of its own first)
+    SplitJobTable jt{};
+    const int kp = kp_of(g.K), tk = cdiv(kp, 64), ta = cdiv(g.M, 32) * tk;
+    jt.jobs[0] = SplitJob{g.A, a_sr, a_sk, reinterpret_cast<__nv_bfloat16*>(ap), g.M, g.K, kp, 0};
+    jt.jobs[1] = SplitJob{g.B, b_sr, b_sk, reinterpret_cast<__nv_bfloat16*>(bp), g.N, g.K, kp, ta};
+    s = split_param_launch(p.pieces, jt, 2, ta + cdiv(g.N, 32) * tk, st);
+  } else {
+    s = split_operand_launch(p.pieces, g.A, a_sr, a_sk, g.M, g.K, ap, st, p.f16);
+    if (s == UGEMM_OK) s = split_operand_launch(p.pieces, g.B, b_sr, b_sk, g.N, g.K, bp, st, p.f16);
+  }
   if (s != UGEMM_OK) return s;
   return split_gemm_on_pieces(g, p, ap, bp, tail_scratch, dev_err, st);
 }
@@ -1933,6 +1994,14 @@ ugemm_status split_operand_launch(int pieces, const float* src, long long sr, lo
   if (f16) {
     if (pieces != 2) return UGEMM_ERR_ARG;
     unsigned* words = split_fmax_word(dst, 2, rows, K);
+    if (sk == 1 && rows > 0 && K > 0 && Kp <= kRowSplitK &&
+        (reinterpret_cast<uintptr_t>(src) & 15) == 0 && (sr & 3) == 0) {
+      // rows contiguous in k: maximum and split in one pass over the operand
+      prof_begin(st);
+      split_rows_f16_kernel<<<rows, 256, 0, st>>>(src, sr, K, Kp, d, rows, words);
+      prof_end(st, kProfSplitPrep);
+      return cudaPeekAtLastError() == cudaSuccess ? UGEMM_OK : UGEMM_ERR_CUDA;
+    }
     if (cudaMemsetAsync(words, 0, sizeof(unsigned) * std::max(rows, 1), st) != cudaSuccess)
       return UGEMM_ERR_CUDA;
     if (rows > 0 && K > 0) {
