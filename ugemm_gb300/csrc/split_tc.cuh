@@ -274,6 +274,7 @@ constexpr int kSplitTableJobs = 8;
 struct SplitJobTable {
   SplitJob jobs[kSplitTableJobs];
 };
+static_assert(sizeof(SplitJobTable) <= 4000, "split job table must fit the kernel parameter space");
 ugemm_status split_param_launch(int pieces, const SplitJobTable& t, int njobs, int total_tiles,
                                 cudaStream_t st);
 ugemm_status split_batched_launch(int pieces, const SplitJob* jobs, int njobs, int total_tiles,
