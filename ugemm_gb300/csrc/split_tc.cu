@@ -337,6 +337,9 @@ __device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
   // is 32 bytes of a row in each: 16 16-bit or 8 tf32 elements
   const uint32_t ifmt = TF32 ? 2u : (NP == 2 && fmt == 1 ? 0u : 1u);
   const uint32_t idesc_full = umma_idesc(ifmt, ifmt, kTcBM, BN);
+  // 128-wide tiles whose first correction is A0 B1: the pair A0 [B0; B1]
+  constexpr bool MERGE = !TF32 && BN == 128 && NPROD >= 3 && corr_code(0) == 0x1;
+  const uint32_t idesc_pair = umma_idesc(ifmt, ifmt, kTcBM, 2 * BN);
   const uint32_t base = smem_u32(smem);
   const uint64_t da0 = umma_smem_desc(base, SBO, SWZ);
   const uint64_t db0 = umma_smem_desc(base + S::A_BYTES, SBO, SWZ);
@@ -375,6 +378,27 @@ __device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
         }
       }
     };
+    // A full-width 128-wide tile's main product and first correction, A0 B0
+    // into the main accumulator and A0 B1 into the correction accumulator
+    // right after it in tensor memory, as one 128 x 256 MMA per k step: the
+    // B0 and B1 planes are adjacent in the stage (rows 0-127 and 128-255 of
+    // one 256-row operand), so A0 is read once for both.  Only where both
+    // accumulate (not at a chunk start, not in a tile's first k-block).
+    auto merged_first = [&](uint32_t st) {
+      const uint64_t so = (st * static_cast<uint32_t>(S::STAGE_BYTES)) >> 4;
+      const uint64_t da = da0 + so, db = db0 + so;
+#pragma unroll
+      for (int kk = 0; kk < KK; ++kk)
+        umma_bf16(t_main, da + ((kk * 32) >> 4), db + ((kk * 32) >> 4), idesc_pair, true);
+#pragma unroll
+      for (int p = 1; p < NPROD - 1; ++p) {
+        const uint32_t ia = corr_code(p) >> 2, ib = corr_code(p) & 3;
+#pragma unroll
+        for (int kk = 0; kk < KK; ++kk)
+          umma_bf16(t_corr, da + ((ia * S::A_PLANE + kk * 32) >> 4),
+                    db + ((ib * S::B_PLANE + kk * 32) >> 4), idesc, true);
+      }
+    };
     auto main_product = [&](uint32_t st, bool restart) {
       const uint64_t so = (st * static_cast<uint32_t>(S::STAGE_BYTES)) >> 4;
       const uint64_t da = da0 + so, db = db0 + so;
@@ -386,9 +410,24 @@ __device__ __forceinline__ void mma_issue_loop(const TcProblem& single,
       }
     };
     int cpos = 0;  // the k-block's position in its chunk
+    const bool pair_ok = MERGE && idesc == idesc_full;
     for (int kb = 0; kb < P.nkb;) {
       if (!mbar_wait(&full[s], ph, err, kDevTimeoutFull)) return;
       tc_fence_after();
+      if (pair_ok && cpos != 0) {
+        merged_first(s);
+        umma_commit(&empty[s]);
+        ++kb;
+        if (++cpos == chunk_kb) {
+          cpos = 0;
+          if (kb < P.nkb) umma_commit(&main_full[buf]);
+        }
+        if (++s == NST) {
+          s = 0;
+          ph ^= 1;
+        }
+        continue;
+      }
       corrections(s, kb);
       // A new chunk restarts the main accumulator once the epilogue has
       // drained the last one.  While that drain runs, the corrections of the
