@@ -269,14 +269,15 @@ def test_fp32_peak_probe_is_a_plausible_rate():
     assert 0.5 * nominal < peak < 1.05 * nominal, (peak, nominal)
 
 
-@pytest.mark.parametrize("K", [1000, 8192, 8200])
+@pytest.mark.parametrize("K", [1000, 1001, 8192, 8200])
 def test_fp16x3_one_pass_row_split_matches_two_pass(K):
     """op(A) with rows contiguous in k (NN, K <= 8192) takes its FP16x3 row
     maxima and pieces in one pass; the same op(A) stored transposed (TN)
     takes the maximum pass and the split pass.  Same words, same pieces:
     C must be bit-identical, including a zero row, a row with an infinity
-    (its maximum ignores it) and a row 2^30 below the others; K = 8200 takes
-    the two passes on both sides."""
+    (its maximum ignores it) and a row 2^30 below the others; an odd K
+    with rows padded by NaNs that must not be read; K = 8200 takes the two
+    passes on both sides."""
     rng = np.random.default_rng(K)
     M, N = 256, 192
     A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
@@ -285,7 +286,12 @@ def test_fp16x3_one_pass_row_split_matches_two_pass(K):
     A[11] *= np.float32(2.0 ** -30)
     B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
     C = rng.uniform(-1, 1, (M, N)).astype(np.float32)
-    nn = run("N", "N", M, N, K, 1.25, A, B, 0.5, C, "fp16x3")
+    # rows padded to a multiple of 4 floats (16-byte aligned), as the one
+    # pass needs; the padding holds garbage that must not be read
+    lda = -(-K // 4) * 4
+    Ap = np.full((M, lda), np.nan, np.float32)
+    Ap[:, :K] = A
+    nn = run("N", "N", M, N, K, 1.25, Ap, B, 0.5, C, "fp16x3", lda=lda)
     tn = run("T", "N", M, N, K, 1.25, np.ascontiguousarray(A.T), B, 0.5, C, "fp16x3", lda=M)
     assert np.array_equal(nn.view(np.int32), tn.view(np.int32))
     finite = np.isfinite(A).all(axis=1)
